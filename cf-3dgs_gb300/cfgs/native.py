@@ -1,0 +1,155 @@
+"""ctypes binding of libcfgs.so (the C ABI declared in include/cfgs.h).
+
+There is no fallback: if the library cannot be loaded, every caller gets an
+ImportError/RuntimeError that says so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+from . import build as _build
+
+STATUS = {
+    0: "CFGS_OK",
+    1: "CFGS_ERR_INVALID_ARGUMENT",
+    2: "CFGS_ERR_CAPACITY",
+    3: "CFGS_ERR_LAUNCH",
+    4: "CFGS_ERR_DEVICE_FLAG",
+    5: "CFGS_ERR_TOO_LARGE",
+}
+FLAG_FRUSTUM_VIOLATION = 0x1
+FLAG_CAPACITY_OVERFLOW = 0x2
+
+_vp = C.c_void_p
+_fp = C.c_void_p  # device float* passed as an address
+
+
+class Settings(C.Structure):
+    _fields_ = [
+        ("image_height", C.c_int32),
+        ("image_width", C.c_int32),
+        ("tanfovx", C.c_float),
+        ("tanfovy", C.c_float),
+        ("bg", _fp),
+        ("scale_modifier", C.c_float),
+        ("viewmatrix", _fp),
+        ("projmatrix", _fp),
+        ("sh_degree", C.c_int32),
+        ("campos", _fp),
+        ("prefiltered", C.c_int32),
+        ("debug", C.c_int32),
+    ]
+
+
+class Gaussians(C.Structure):
+    _fields_ = [
+        ("num_gaussians", C.c_int32),
+        ("means3D", _fp),
+        ("opacities", _fp),
+        ("shs", _fp),
+        ("sh_coeffs", C.c_int32),
+        ("colors_precomp", _fp),
+        ("scales", _fp),
+        ("rotations", _fp),
+        ("cov3D_precomp", _fp),
+    ]
+
+
+class Gradients(C.Structure):
+    _fields_ = [
+        ("dL_dmeans2D", _fp),
+        ("dL_dcolors", _fp),
+        ("dL_dopacity", _fp),
+        ("dL_dmeans3D", _fp),
+        ("dL_dcov3D", _fp),
+        ("dL_dsh", _fp),
+        ("dL_dscales", _fp),
+        ("dL_drotations", _fp),
+    ]
+
+
+class Counts(C.Structure):
+    _fields_ = [("num_rendered", C.c_uint32), ("flags", C.c_uint32)]
+
+
+EXPORTS = {
+    # name: (restype, argtypes)
+    "cfgs_geom_bytes": (C.c_size_t, [C.c_int32]),
+    "cfgs_image_bytes": (C.c_size_t, [C.c_int32, C.c_int32]),
+    "cfgs_binning_bytes": (C.c_size_t, [C.c_int64]),
+    "cfgs_backward_scratch_bytes": (C.c_size_t, [C.c_int64]),
+    "cfgs_geom_layout": (None, [C.c_int32, C.POINTER(C.c_size_t)]),
+    "cfgs_image_layout": (None, [C.c_int32, C.c_int32, C.POINTER(C.c_size_t)]),
+    "cfgs_binning_layout": (None, [C.c_int64, C.POINTER(C.c_size_t)]),
+    "cfgs_preprocess_forward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, _vp]),
+    "cfgs_read_counts": (C.c_int, [_vp, C.POINTER(Counts), _vp]),
+    "cfgs_render_forward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, C.c_int64,
+                                      _vp, _vp, _vp, _vp]),
+    "cfgs_backward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, _vp, C.c_int64, _vp,
+                                _vp, _vp, _vp, C.POINTER(Gradients), _vp]),
+    "cfgs_mark_visible": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp]),
+    "cfgs_pose_apply": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "cfgs_pose_scratch_bytes": (C.c_size_t, [C.c_int32]),
+    "cfgs_pose_grad": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "cfgs_pose_adam": (C.c_int, [_vp, _vp, _vp, C.c_float, C.c_float, C.c_float, C.c_float, _vp]),
+}
+
+_LIB = None
+
+
+def lib_path() -> Path:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Loads libcfgs.so (building it first when it is missing or stale)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB_PATH
+    if build_if_missing and (not path.exists() or os.environ.get("CFGS_NO_BUILD") != "1"):
+        try:
+            path = _build.build()
+        except Exception as e:  # the toolkit is needed; say so instead of limping on
+            if not path.exists():
+                raise ImportError(f"libcfgs.so is missing and could not be built: {e}") from e
+    if not path.exists():
+        raise ImportError(f"libcfgs.so not found at {path}; run __graft_entry__.build()")
+    lib = C.CDLL(str(path))
+    for name, (res, args) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        raise RuntimeError(f"{what} failed: {STATUS.get(status, status)}")
+
+
+GEOM_FIELDS = ["xy", "conic_op", "rgbd", "rect", "touched", "offset", "clamped", "block_sums", "block_prefix",
+               "total"]
+IMAGE_FIELDS = ["counts", "tile_count", "tile_range", "tile_cursor", "final_T", "n_contrib", "total"]
+BINNING_FIELDS = ["keys", "keys_alt", "inst_gid", "sorted_gid", "sorted_pidx", "total"]
+
+
+def geom_layout(n: int) -> dict:
+    arr = (C.c_size_t * 10)()
+    load().cfgs_geom_layout(int(n), arr)
+    return dict(zip(GEOM_FIELDS, list(arr)))
+
+
+def image_layout(w: int, h: int) -> dict:
+    arr = (C.c_size_t * 7)()
+    load().cfgs_image_layout(int(w), int(h), arr)
+    return dict(zip(IMAGE_FIELDS, list(arr)))
+
+
+def binning_layout(cap: int) -> dict:
+    arr = (C.c_size_t * 6)()
+    load().cfgs_binning_layout(int(cap), arr)
+    return dict(zip(BINNING_FIELDS, list(arr)))

@@ -1,0 +1,223 @@
+// Internal definitions shared by the rasteriser translation units: workspace
+// layouts, launch helpers and the scalar math whose rounding the CPU oracle mirrors.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/cfgs.h"
+
+namespace cfgs {
+
+constexpr int kTileX = CFGS_TILE_X;
+constexpr int kTileY = CFGS_TILE_Y;
+constexpr int kTilePixels = kTileX * kTileY;  // 256
+constexpr int kPreprocessBlock = 256;
+constexpr int kMaxShCoeffs = 16;  // SH degree 3
+
+// ---------------------------------------------------------------------------
+// Workspace layouts. Every array starts on a 256-byte boundary.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct GeomLayout {
+  size_t xy, conic_op, rgbd, rect, touched, offset, clamped, block_sums, block_prefix, total;
+  int32_t num_blocks;
+  __host__ __device__ explicit GeomLayout(int32_t n) {
+    num_blocks = (n + kPreprocessBlock - 1) / kPreprocessBlock;
+    size_t o = 0;
+    xy = o;           o = align256(o + sizeof(float) * 2 * (size_t)n);
+    conic_op = o;     o = align256(o + sizeof(float) * 4 * (size_t)n);
+    rgbd = o;         o = align256(o + sizeof(float) * 4 * (size_t)n);
+    rect = o;         o = align256(o + sizeof(uint32_t) * 2 * (size_t)n);
+    touched = o;      o = align256(o + sizeof(uint32_t) * (size_t)n);
+    offset = o;       o = align256(o + sizeof(uint32_t) * (size_t)n);
+    clamped = o;      o = align256(o + (size_t)n);
+    block_sums = o;   o = align256(o + sizeof(uint32_t) * (size_t)(num_blocks + 1));
+    block_prefix = o; o = align256(o + sizeof(uint32_t) * (size_t)(num_blocks + 1));
+    total = o;
+  }
+};
+
+struct GeomView {
+  float2* xy;          // pixel-space centre
+  float4* conic_op;    // (conic a, conic b, conic c, opacity)
+  float4* rgbd;        // (r, g, b, view depth)
+  uint2* rect;         // (min_x | min_y << 16, max_x | max_y << 16) in tiles
+  uint32_t* touched;   // tiles touched (0 = culled)
+  uint32_t* offset;    // exclusive prefix of touched = first pre-sort instance index
+  uint8_t* clamped;    // bit c set: SH colour channel c was clamped at 0
+  uint32_t* block_sums;
+  uint32_t* block_prefix;
+  __host__ __device__ GeomView() {}
+  __host__ __device__ GeomView(void* base, int32_t n) {
+    GeomLayout L(n);
+    char* b = static_cast<char*>(base);
+    xy = reinterpret_cast<float2*>(b + L.xy);
+    conic_op = reinterpret_cast<float4*>(b + L.conic_op);
+    rgbd = reinterpret_cast<float4*>(b + L.rgbd);
+    rect = reinterpret_cast<uint2*>(b + L.rect);
+    touched = reinterpret_cast<uint32_t*>(b + L.touched);
+    offset = reinterpret_cast<uint32_t*>(b + L.offset);
+    clamped = reinterpret_cast<uint8_t*>(b + L.clamped);
+    block_sums = reinterpret_cast<uint32_t*>(b + L.block_sums);
+    block_prefix = reinterpret_cast<uint32_t*>(b + L.block_prefix);
+  }
+};
+
+struct ImageLayout {
+  size_t header, tile_count, tile_range, tile_cursor, final_T, n_contrib, total;
+  int32_t grid_x, grid_y, num_tiles;
+  __host__ __device__ ImageLayout(int32_t w, int32_t h) {
+    grid_x = (w + kTileX - 1) / kTileX;
+    grid_y = (h + kTileY - 1) / kTileY;
+    num_tiles = grid_x * grid_y;
+    size_t px = (size_t)w * (size_t)h;
+    size_t o = 0;
+    header = o;      o = align256(o + sizeof(CfgsCounts));
+    tile_count = o;  o = align256(o + sizeof(uint32_t) * (size_t)num_tiles);
+    tile_range = o;  o = align256(o + sizeof(uint32_t) * (size_t)(num_tiles + 1));
+    tile_cursor = o; o = align256(o + sizeof(uint32_t) * (size_t)num_tiles);
+    final_T = o;     o = align256(o + sizeof(float) * px);
+    n_contrib = o;   o = align256(o + sizeof(uint32_t) * px);
+    total = o;
+  }
+};
+
+struct ImageView {
+  CfgsCounts* counts;
+  uint32_t* tile_count;
+  uint32_t* tile_range;   // [num_tiles + 1]: tile t owns sorted positions [r[t], r[t+1])
+  uint32_t* tile_cursor;
+  float* final_T;
+  uint32_t* n_contrib;
+  __host__ __device__ ImageView() {}
+  __host__ __device__ ImageView(void* base, int32_t w, int32_t h) {
+    ImageLayout L(w, h);
+    char* b = static_cast<char*>(base);
+    counts = reinterpret_cast<CfgsCounts*>(b + L.header);
+    tile_count = reinterpret_cast<uint32_t*>(b + L.tile_count);
+    tile_range = reinterpret_cast<uint32_t*>(b + L.tile_range);
+    tile_cursor = reinterpret_cast<uint32_t*>(b + L.tile_cursor);
+    final_T = reinterpret_cast<float*>(b + L.final_T);
+    n_contrib = reinterpret_cast<uint32_t*>(b + L.n_contrib);
+  }
+};
+
+struct BinningLayout {
+  size_t keys, keys_alt, inst_gid, sorted_gid, sorted_pidx, total;
+  __host__ __device__ explicit BinningLayout(int64_t cap) {
+    size_t c = cap > 0 ? (size_t)cap : 1;
+    size_t o = 0;
+    keys = o;        o = align256(o + sizeof(uint64_t) * c);
+    keys_alt = o;    o = align256(o + sizeof(uint64_t) * c);
+    inst_gid = o;    o = align256(o + sizeof(uint32_t) * c);
+    sorted_gid = o;  o = align256(o + sizeof(uint32_t) * c);
+    sorted_pidx = o; o = align256(o + sizeof(uint32_t) * c);
+    total = o;
+  }
+};
+
+struct BinningView {
+  uint64_t* keys;        // (depth bits << 32 | pre-sort instance index), bucketed by tile
+  uint64_t* keys_alt;    // ping-pong buffer of the large-tile merge
+  uint32_t* inst_gid;    // pre-sort instance index -> Gaussian id
+  uint32_t* sorted_gid;  // sorted position -> Gaussian id
+  uint32_t* sorted_pidx; // sorted position -> pre-sort instance index
+  __host__ __device__ BinningView() {}
+  __host__ __device__ BinningView(void* base, int64_t cap) {
+    BinningLayout L(cap);
+    char* b = static_cast<char*>(base);
+    keys = reinterpret_cast<uint64_t*>(b + L.keys);
+    keys_alt = reinterpret_cast<uint64_t*>(b + L.keys_alt);
+    inst_gid = reinterpret_cast<uint32_t*>(b + L.inst_gid);
+    sorted_gid = reinterpret_cast<uint32_t*>(b + L.sorted_gid);
+    sorted_pidx = reinterpret_cast<uint32_t*>(b + L.sorted_pidx);
+  }
+};
+
+// Backward scratch: one 48-byte record per pre-sort instance:
+// (dxy.x, dxy.y, dconic.a, dconic.b) (dconic.c, dopacity, drgb.r, drgb.g) (drgb.b, ddepth, 0, 0)
+constexpr int kRecordFloat4 = 3;
+
+// ---------------------------------------------------------------------------
+// Scalar math whose exact rounding sequence the CPU oracle reproduces.
+// ---------------------------------------------------------------------------
+
+// exp(x) in float: Cody–Waite reduction x = k ln2 + r (|r| <= ln2/2) with ln2 split
+// into a 15-bit head (so k*head is exact) and a tail, then the degree-7 Taylor
+// polynomial of e^r in Horner form (truncation error < 1e-8 relative), then an
+// exact two-step scaling by 2^k. Every operation is an IEEE-rounded float op or an
+// fma, so the same sequence in C gives the same bits.
+__device__ __forceinline__ float exp_ref(float x) {
+  if (x != x) return x;
+  if (x < -104.0f) return 0.0f;
+  if (x > 88.75f) return __int_as_float(0x7f800000);
+  const float kLog2e = 1.4426950216293335f;
+  const float kLn2Hi = 0.693145751953125f;
+  const float kLn2Lo = 1.428606765330187e-06f;
+  float kf = rintf(x * kLog2e);
+  float r = fmaf(-kf, kLn2Hi, x);
+  r = fmaf(-kf, kLn2Lo, r);
+  float p = 0.00019841270113829523f;
+  p = fmaf(p, r, 0.0013888889225199819f);
+  p = fmaf(p, r, 0.008333333767950535f);
+  p = fmaf(p, r, 0.0416666679084301f);
+  p = fmaf(p, r, 0.1666666716337204f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  int k = (int)kf;
+  int k1 = k >> 1;
+  int k2 = k - k1;
+  float s1 = __int_as_float((k1 + 127) << 23);
+  float s2 = __int_as_float((k2 + 127) << 23);
+  return (p * s1) * s2;
+}
+
+// Exponent of the 2D Gaussian at pixel offset (dx, dy) = (mean - pixel), with the
+// per-Gaussian factors pre-scaled as ca = -conic.a/2, cb = -conic.b, cc = -conic.c/2:
+// power = ca dx^2 + cb dx dy + cc dy^2, evaluated in this exact order. Shared by the
+// forward and backward render so the backward replays the forward's skip decisions.
+__device__ __forceinline__ float gauss_power(float ca, float cb, float cc, float dx, float dy) {
+  float e = cb * (dx * dy);
+  e = fmaf(cc * dy, dy, e);
+  return fmaf(ca * dx, dx, e);
+}
+
+// Real spherical-harmonics constants of utils/sh_utils.py:16-40 (degrees 0..3).
+#define CFGS_SH_C0 0.28209479177387814f
+#define CFGS_SH_C1 0.4886025119029199f
+#define CFGS_SH_C2_0 1.0925484305920792f
+#define CFGS_SH_C2_1 (-1.0925484305920792f)
+#define CFGS_SH_C2_2 0.31539156525252005f
+#define CFGS_SH_C2_3 (-1.0925484305920792f)
+#define CFGS_SH_C2_4 0.5462742152960396f
+#define CFGS_SH_C3_0 (-0.5900435899266435f)
+#define CFGS_SH_C3_1 2.890611442640554f
+#define CFGS_SH_C3_2 (-0.4570457994644658f)
+#define CFGS_SH_C3_3 0.3731763325901154f
+#define CFGS_SH_C3_4 (-0.4570457994644658f)
+#define CFGS_SH_C3_5 1.445305721320277f
+#define CFGS_SH_C3_6 (-0.5900435899266435f)
+
+// Alpha-compositing thresholds of the published 3DGS rasteriser.
+#define CFGS_ALPHA_MAX 0.99f
+#define CFGS_ALPHA_MIN 0.003921568859368563f  // 1/255 in float
+#define CFGS_T_MIN 0.0001f
+#define CFGS_NEAR_Z 0.2f
+
+inline int div_up(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Host-side launch check; returns CFGS_ERR_LAUNCH from the calling entry point.
+#define CFGS_CHECK_LAUNCH(settings_debug, stream)                       \
+  do {                                                                  \
+    cudaError_t e_ = cudaGetLastError();                                \
+    if (e_ != cudaSuccess) return CFGS_ERR_LAUNCH;                      \
+    if (settings_debug) {                                               \
+      e_ = cudaStreamSynchronize((cudaStream_t)(stream));               \
+      if (e_ != cudaSuccess) return CFGS_ERR_LAUNCH;                    \
+    }                                                                   \
+  } while (0)
+
+}  // namespace cfgs

@@ -1,0 +1,426 @@
+// Forward phase 1: per-Gaussian preprocess (EWA projection, SH colour, radius, tile
+// rectangle), per-tile instance counts and the two scans. Also markVisible.
+//
+// This translation unit is compiled with -fmad=false: every a*b+c below is two
+// IEEE-rounded operations unless written as fmaf(), so the CPU oracle reproduces the
+// outputs (radii, rectangles, depth keys, conics) bit for bit.
+//
+// Algorithm: the published 3DGS preprocess (EWA splatting, Zwicker et al. 2001, with
+// the 3DGS low-pass of 0.3 px^2 and the 1.3*tan(fov) Jacobian clamp), restated. The
+// reference's Python statements of the same math are utils/general_utils.py:76-108
+// (covariance), utils/sh_utils.py:57-112 (SH), scene/cameras.py:57-74 and
+// utils/graphics_utils.py:85-113 (camera matrices).
+#include "cfgs_internal.cuh"
+
+namespace cfgs {
+
+struct CamConst {
+  float V[16];
+  float P[16];
+  float campos[3];
+};
+
+__device__ __forceinline__ void load_cam(const CfgsSettings& s, CamConst& c) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) c.V[i] = __ldg(s.viewmatrix + i);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) c.P[i] = __ldg(s.projmatrix + i);
+  if (s.campos) {
+    c.campos[0] = __ldg(s.campos + 0);
+    c.campos[1] = __ldg(s.campos + 1);
+    c.campos[2] = __ldg(s.campos + 2);
+  } else {
+    c.campos[0] = c.campos[1] = c.campos[2] = 0.f;
+  }
+}
+
+// [p,1] @ M, columns 0..2 (row-vector convention of the stored matrices).
+__device__ __forceinline__ float3 xform43(const float* m, float3 p) {
+  float3 r;
+  r.x = fmaf(m[8], p.z, fmaf(m[4], p.y, fmaf(m[0], p.x, m[12])));
+  r.y = fmaf(m[9], p.z, fmaf(m[5], p.y, fmaf(m[1], p.x, m[13])));
+  r.z = fmaf(m[10], p.z, fmaf(m[6], p.y, fmaf(m[2], p.x, m[14])));
+  return r;
+}
+__device__ __forceinline__ float xform_w(const float* m, float3 p) {
+  return fmaf(m[11], p.z, fmaf(m[7], p.y, fmaf(m[3], p.x, m[15])));
+}
+
+// Sigma = R diag(s)^2 R^T with R the rotation of quaternion (r,x,y,z) (not
+// normalised here; CF-3DGS normalises in Python), stored (xx,xy,xz,yy,yz,zz).
+__device__ __forceinline__ void cov3d_from_scale_rot(float3 s, float mod, float4 q, float* cov) {
+  float sx = mod * s.x, sy = mod * s.y, sz = mod * s.z;
+  float r = q.x, x = q.y, y = q.z, z = q.w;
+  float xx = x * x, yy = y * y, zz = z * z;
+  float xy = x * y, xz = x * z, yz = y * z;
+  float rx = r * x, ry = r * y, rz = r * z;
+  float R[9];
+  R[0] = 1.0f - 2.0f * (yy + zz);
+  R[1] = 2.0f * (xy - rz);
+  R[2] = 2.0f * (xz + ry);
+  R[3] = 2.0f * (xy + rz);
+  R[4] = 1.0f - 2.0f * (xx + zz);
+  R[5] = 2.0f * (yz - rx);
+  R[6] = 2.0f * (xz - ry);
+  R[7] = 2.0f * (yz + rx);
+  R[8] = 1.0f - 2.0f * (xx + yy);
+  float M[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    M[3 * i + 0] = R[3 * i + 0] * sx;
+    M[3 * i + 1] = R[3 * i + 1] * sy;
+    M[3 * i + 2] = R[3 * i + 2] * sz;
+  }
+  const int ii[6] = {0, 0, 0, 1, 1, 2};
+  const int jj[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const float* a = M + 3 * ii[k];
+    const float* b = M + 3 * jj[k];
+    cov[k] = fmaf(a[2], b[2], fmaf(a[1], b[1], a[0] * b[0]));
+  }
+}
+
+// 2D screen covariance (a, b, c) = J W Sigma W^T J^T + 0.3 I.
+__device__ __forceinline__ float3 cov2d(float3 t, float fx, float fy, float tanfovx, float tanfovy,
+                                        const float* cov, const float* V) {
+  float limx = 1.3f * tanfovx;
+  float limy = 1.3f * tanfovy;
+  float txtz = t.x / t.z;
+  float tytz = t.y / t.z;
+  float tx = fminf(limx, fmaxf(-limx, txtz)) * t.z;
+  float ty = fminf(limy, fmaxf(-limy, tytz)) * t.z;
+  float tz2 = t.z * t.z;
+  float J00 = fx / t.z;
+  float J02 = -(fx * tx) / tz2;
+  float J11 = fy / t.z;
+  float J12 = -(fy * ty) / tz2;
+  // W[i][j] = V[4j+i]; rows of T = J W.
+  float T0[3], T1[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    T0[j] = fmaf(J02, V[4 * j + 2], J00 * V[4 * j + 0]);
+    T1[j] = fmaf(J12, V[4 * j + 2], J11 * V[4 * j + 1]);
+  }
+  float S[9] = {cov[0], cov[1], cov[2], cov[1], cov[3], cov[4], cov[2], cov[4], cov[5]};
+  float u[3], v[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    u[i] = fmaf(S[3 * i + 2], T0[2], fmaf(S[3 * i + 1], T0[1], S[3 * i + 0] * T0[0]));
+    v[i] = fmaf(S[3 * i + 2], T1[2], fmaf(S[3 * i + 1], T1[1], S[3 * i + 0] * T1[0]));
+  }
+  float a = fmaf(T0[2], u[2], fmaf(T0[1], u[1], T0[0] * u[0]));
+  float b = fmaf(T0[2], v[2], fmaf(T0[1], v[1], T0[0] * v[0]));
+  float c = fmaf(T1[2], v[2], fmaf(T1[1], v[1], T1[0] * v[0]));
+  return make_float3(a + 0.3f, b, c + 0.3f);
+}
+
+__device__ __forceinline__ float ndc2pix(float v, int S) { return ((v + 1.0f) * (float)S - 1.0f) * 0.5f; }
+
+// Colour from real SH of degree <= 3 at the view direction, + 0.5, clamped at 0.
+__device__ __forceinline__ float3 sh_to_rgb(int deg, const float* sh, float3 p, const float* campos,
+                                            uint8_t* clamped) {
+  float dx = p.x - campos[0], dy = p.y - campos[1], dz = p.z - campos[2];
+  float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+  float x = dx / len, y = dy / len, z = dz / len;
+  float b[kMaxShCoeffs];
+  b[0] = CFGS_SH_C0;
+  int nb = 1;
+  if (deg > 0) {
+    b[1] = -CFGS_SH_C1 * y;
+    b[2] = CFGS_SH_C1 * z;
+    b[3] = -CFGS_SH_C1 * x;
+    nb = 4;
+    if (deg > 1) {
+      float xx = x * x, yy = y * y, zz = z * z;
+      float xy = x * y, yz = y * z, xz = x * z;
+      b[4] = CFGS_SH_C2_0 * xy;
+      b[5] = CFGS_SH_C2_1 * yz;
+      b[6] = CFGS_SH_C2_2 * ((2.0f * zz - xx) - yy);
+      b[7] = CFGS_SH_C2_3 * xz;
+      b[8] = CFGS_SH_C2_4 * (xx - yy);
+      nb = 9;
+      if (deg > 2) {
+        b[9] = (CFGS_SH_C3_0 * y) * (3.0f * xx - yy);
+        b[10] = (CFGS_SH_C3_1 * xy) * z;
+        b[11] = (CFGS_SH_C3_2 * y) * ((4.0f * zz - xx) - yy);
+        b[12] = (CFGS_SH_C3_3 * z) * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
+        b[13] = (CFGS_SH_C3_4 * x) * ((4.0f * zz - xx) - yy);
+        b[14] = (CFGS_SH_C3_5 * z) * (xx - yy);
+        b[15] = (CFGS_SH_C3_6 * x) * (xx - 3.0f * yy);
+        nb = 16;
+      }
+    }
+  }
+  float r = b[0] * sh[0], g = b[0] * sh[1], bl = b[0] * sh[2];
+#pragma unroll
+  for (int k = 1; k < kMaxShCoeffs; ++k) {
+    if (k < nb) {
+      r = fmaf(b[k], sh[3 * k + 0], r);
+      g = fmaf(b[k], sh[3 * k + 1], g);
+      bl = fmaf(b[k], sh[3 * k + 2], bl);
+    }
+  }
+  r = r + 0.5f;
+  g = g + 0.5f;
+  bl = bl + 0.5f;
+  *clamped = (uint8_t)((r < 0.0f ? 1 : 0) | (g < 0.0f ? 2 : 0) | (bl < 0.0f ? 4 : 0));
+  return make_float3(fmaxf(r, 0.0f), fmaxf(g, 0.0f), fmaxf(bl, 0.0f));
+}
+
+struct PreArgs {
+  CfgsSettings s;
+  CfgsGaussians g;
+  GeomView geom;
+  uint32_t* tile_count;
+  CfgsCounts* counts;
+  int32_t* radii;
+  int grid_x, grid_y;
+  float focal_x, focal_y;
+};
+
+__device__ __forceinline__ uint32_t block_reduce_sum_u32(uint32_t v, uint32_t* sh_warp) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sh_warp[warp] = v;
+  __syncthreads();
+  uint32_t t = 0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sh_warp[w];
+  }
+  return t;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs a) {
+  __shared__ uint32_t sh_warp[kPreprocessBlock / 32];
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int N = a.g.num_gaussians;
+  uint32_t touched = 0;
+  if (idx < N) {
+    int radius = 0;
+    CamConst cam;
+    load_cam(a.s, cam);
+    const float* mp = a.g.means3D + 3 * (size_t)idx;
+    float3 p = make_float3(mp[0], mp[1], mp[2]);
+    float3 t = xform43(cam.V, p);
+    bool culled = t.z <= CFGS_NEAR_Z;
+    if (culled && a.s.prefiltered) atomicOr(&a.counts->flags, CFGS_FLAG_FRUSTUM_VIOLATION);
+    if (!culled) {
+      float3 hom = xform43(cam.P, p);
+      float hw = xform_w(cam.P, p);
+      float w_inv = 1.0f / (hw + 0.0000001f);
+      float3 proj = make_float3(hom.x * w_inv, hom.y * w_inv, hom.z * w_inv);
+      float cov[6];
+      if (a.g.cov3D_precomp) {
+        const float* c = a.g.cov3D_precomp + 6 * (size_t)idx;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) cov[k] = c[k];
+      } else {
+        const float* s = a.g.scales + 3 * (size_t)idx;
+        const float* qp = a.g.rotations + 4 * (size_t)idx;
+        float4 q = make_float4(qp[0], qp[1], qp[2], qp[3]);
+        cov3d_from_scale_rot(make_float3(s[0], s[1], s[2]), a.s.scale_modifier, q, cov);
+      }
+      float3 c2 = cov2d(t, a.focal_x, a.focal_y, a.s.tanfovx, a.s.tanfovy, cov, cam.V);
+      float det = c2.x * c2.z - c2.y * c2.y;
+      if (det != 0.0f) {
+        float det_inv = 1.0f / det;
+        float3 conic = make_float3(c2.z * det_inv, -c2.y * det_inv, c2.x * det_inv);
+        float mid = 0.5f * (c2.x + c2.z);
+        float disc = sqrtf(fmaxf(0.1f, mid * mid - det));
+        float l1 = mid + disc, l2 = mid - disc;
+        float rad_f = ceilf(3.0f * sqrtf(fmaxf(l1, l2)));
+        int rad = (int)rad_f;
+        float2 pimg = make_float2(ndc2pix(proj.x, a.s.image_width), ndc2pix(proj.y, a.s.image_height));
+        float rf = (float)rad;
+        int rminx = min(a.grid_x, max(0, (int)((pimg.x - rf) / (float)kTileX)));
+        int rminy = min(a.grid_y, max(0, (int)((pimg.y - rf) / (float)kTileY)));
+        int rmaxx = min(a.grid_x, max(0, (int)(((pimg.x + rf) + (float)(kTileX - 1)) / (float)kTileX)));
+        int rmaxy = min(a.grid_y, max(0, (int)(((pimg.y + rf) + (float)(kTileY - 1)) / (float)kTileY)));
+        uint32_t area = (uint32_t)((rmaxx - rminx) * (rmaxy - rminy));
+        if (area > 0) {
+          float3 rgb;
+          uint8_t cl = 0;
+          if (a.g.colors_precomp) {
+            const float* c = a.g.colors_precomp + 3 * (size_t)idx;
+            rgb = make_float3(c[0], c[1], c[2]);
+          } else {
+            rgb = sh_to_rgb(a.s.sh_degree, a.g.shs + (size_t)idx * a.g.sh_coeffs * 3, p, cam.campos, &cl);
+          }
+          a.geom.xy[idx] = pimg;
+          a.geom.conic_op[idx] = make_float4(conic.x, conic.y, conic.z, a.g.opacities[idx]);
+          a.geom.rgbd[idx] = make_float4(rgb.x, rgb.y, rgb.z, t.z);
+          a.geom.rect[idx] = make_uint2((uint32_t)rminx | ((uint32_t)rminy << 16),
+                                        (uint32_t)rmaxx | ((uint32_t)rmaxy << 16));
+          a.geom.clamped[idx] = cl;
+          touched = area;
+          radius = rad;
+          for (int ty = rminy; ty < rmaxy; ++ty)
+            for (int tx = rminx; tx < rmaxx; ++tx) atomicAdd(&a.tile_count[ty * a.grid_x + tx], 1u);
+        }
+      }
+    }
+    a.radii[idx] = radius;
+    a.geom.touched[idx] = touched;
+  }
+  uint32_t bs = block_reduce_sum_u32(touched, sh_warp);
+  if (threadIdx.x == 0) a.geom.block_sums[blockIdx.x] = bs;
+}
+
+// Exclusive scan of `n` uint32 values by one block of 1024 threads; returns the total.
+__device__ uint64_t block_exclusive_scan(const uint32_t* in, uint32_t* out, int n, uint32_t* sh) {
+  uint64_t carry = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = 0; base < n; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    uint32_t v = i < n ? in[i] : 0u;
+    uint32_t x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0u;
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      sh[32 + lane] = w;  // inclusive warp totals
+    }
+    __syncthreads();
+    uint32_t warp_prefix = warp > 0 ? sh[32 + warp - 1] : 0u;
+    uint64_t excl = carry + warp_prefix + (x - v);
+    if (i < n) out[i] = (uint32_t)excl;
+    uint32_t chunk_total = sh[32 + (blockDim.x >> 5) - 1];
+    __syncthreads();
+    carry += chunk_total;
+  }
+  return carry;
+}
+
+// One block: tile counts -> tile ranges (K), block sums -> block prefixes.
+__global__ void __launch_bounds__(1024) k_scan(uint32_t* tile_count, uint32_t* tile_range,
+                                               uint32_t* tile_cursor, int num_tiles,
+                                               uint32_t* block_sums, uint32_t* block_prefix,
+                                               int num_blocks, CfgsCounts* counts) {
+  __shared__ uint32_t sh[64];
+  uint64_t K = block_exclusive_scan(tile_count, tile_range, num_tiles, sh);
+  for (int i = threadIdx.x; i < num_tiles; i += blockDim.x) tile_cursor[i] = 0u;
+  if (threadIdx.x == 0) {
+    uint32_t k32 = K > 0xffffffffull ? 0xffffffffu : (uint32_t)K;
+    tile_range[num_tiles] = k32;
+    counts->num_rendered = k32;
+    if (K > 0x7fffffffull) atomicOr(&counts->flags, CFGS_FLAG_CAPACITY_OVERFLOW);
+  }
+  block_exclusive_scan(block_sums, block_prefix, num_blocks, sh);
+}
+
+__global__ void __launch_bounds__(256) k_mark_visible(int n, const float* means, const float* V,
+                                                      uint8_t* vis) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float m[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) m[k] = __ldg(V + k);
+  float3 p = make_float3(means[3 * i], means[3 * i + 1], means[3 * i + 2]);
+  float3 t = xform43(m, p);
+  vis[i] = t.z <= CFGS_NEAR_Z ? 0 : 1;
+}
+
+}  // namespace cfgs
+
+using namespace cfgs;
+
+extern "C" size_t cfgs_geom_bytes(int32_t n) { return n < 0 ? 0 : GeomLayout(n).total; }
+extern "C" size_t cfgs_image_bytes(int32_t w, int32_t h) {
+  return (w <= 0 || h <= 0) ? 0 : ImageLayout(w, h).total;
+}
+extern "C" size_t cfgs_binning_bytes(int64_t cap) { return cap < 0 ? 0 : BinningLayout(cap).total; }
+extern "C" size_t cfgs_backward_scratch_bytes(int64_t cap) {
+  return align256(sizeof(float) * 4 * kRecordFloat4 * (size_t)(cap > 0 ? cap : 1));
+}
+
+extern "C" void cfgs_geom_layout(int32_t n, size_t o[10]) {
+  GeomLayout L(n < 0 ? 0 : n);
+  size_t v[10] = {L.xy, L.conic_op, L.rgbd, L.rect, L.touched, L.offset, L.clamped, L.block_sums, L.block_prefix,
+                  L.total};
+  for (int i = 0; i < 10; ++i) o[i] = v[i];
+}
+extern "C" void cfgs_image_layout(int32_t w, int32_t h, size_t o[7]) {
+  ImageLayout L(w < 1 ? 1 : w, h < 1 ? 1 : h);
+  size_t v[7] = {L.header, L.tile_count, L.tile_range, L.tile_cursor, L.final_T, L.n_contrib, L.total};
+  for (int i = 0; i < 7; ++i) o[i] = v[i];
+}
+extern "C" void cfgs_binning_layout(int64_t cap, size_t o[6]) {
+  BinningLayout L(cap);
+  size_t v[6] = {L.keys, L.keys_alt, L.inst_gid, L.sorted_gid, L.sorted_pidx, L.total};
+  for (int i = 0; i < 6; ++i) o[i] = v[i];
+}
+
+static bool settings_ok(const CfgsSettings* s) {
+  return s && s->image_width > 0 && s->image_height > 0 && s->viewmatrix && s->projmatrix &&
+         s->bg && s->sh_degree >= 0 && s->sh_degree <= 3 && s->image_width <= 65535 * kTileX &&
+         s->image_height <= 65535 * kTileY;
+}
+
+extern "C" int cfgs_preprocess_forward(const CfgsSettings* s, const CfgsGaussians* g, void* geom,
+                                       void* image, int32_t* radii, void* stream) {
+  if (!settings_ok(s) || !g || !geom || !image || !radii) return CFGS_ERR_INVALID_ARGUMENT;
+  if (g->num_gaussians < 0) return CFGS_ERR_INVALID_ARGUMENT;
+  if (g->num_gaussians > 0) {
+    if (!g->means3D || !g->opacities) return CFGS_ERR_INVALID_ARGUMENT;
+    if ((g->shs == nullptr) == (g->colors_precomp == nullptr)) return CFGS_ERR_INVALID_ARGUMENT;
+    if (g->cov3D_precomp == nullptr && (g->scales == nullptr || g->rotations == nullptr))
+      return CFGS_ERR_INVALID_ARGUMENT;
+    if (g->shs && g->sh_coeffs < (s->sh_degree + 1) * (s->sh_degree + 1)) return CFGS_ERR_INVALID_ARGUMENT;
+    if (g->shs && !s->campos) return CFGS_ERR_INVALID_ARGUMENT;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  ImageLayout IL(s->image_width, s->image_height);
+  ImageView iv(image, s->image_width, s->image_height);
+  GeomView gv(geom, g->num_gaussians);
+  GeomLayout GL(g->num_gaussians);
+  if (cudaMemsetAsync(iv.counts, 0, sizeof(CfgsCounts), st) != cudaSuccess) return CFGS_ERR_LAUNCH;
+  if (cudaMemsetAsync(iv.tile_count, 0, sizeof(uint32_t) * IL.num_tiles, st) != cudaSuccess)
+    return CFGS_ERR_LAUNCH;
+  if (g->num_gaussians > 0) {
+    PreArgs a;
+    a.s = *s;
+    a.g = *g;
+    a.geom = gv;
+    a.tile_count = iv.tile_count;
+    a.counts = iv.counts;
+    a.radii = radii;
+    a.grid_x = IL.grid_x;
+    a.grid_y = IL.grid_y;
+    a.focal_x = (float)s->image_width / (2.0f * s->tanfovx);
+    a.focal_y = (float)s->image_height / (2.0f * s->tanfovy);
+    k_preprocess<<<GL.num_blocks, kPreprocessBlock, 0, st>>>(a);
+    CFGS_CHECK_LAUNCH(s->debug, st);
+  }
+  k_scan<<<1, 1024, 0, st>>>(iv.tile_count, iv.tile_range, iv.tile_cursor, IL.num_tiles,
+                             gv.block_sums, gv.block_prefix, GL.num_blocks, iv.counts);
+  CFGS_CHECK_LAUNCH(s->debug, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_read_counts(const void* image, CfgsCounts* out, void* stream) {
+  if (!image || !out) return CFGS_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(out, image, sizeof(CfgsCounts), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return CFGS_ERR_LAUNCH;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return CFGS_ERR_LAUNCH;
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_mark_visible(int32_t n, const float* means3D, const float* viewmatrix,
+                                 const float* projmatrix, uint8_t* visible, void* stream) {
+  (void)projmatrix;
+  if (n < 0 || (n > 0 && (!means3D || !viewmatrix || !visible))) return CFGS_ERR_INVALID_ARGUMENT;
+  if (n == 0) return CFGS_OK;
+  k_mark_visible<<<div_up(n, 256), 256, 0, (cudaStream_t)stream>>>(n, means3D, viewmatrix, visible);
+  CFGS_CHECK_LAUNCH(0, stream);
+  return CFGS_OK;
+}

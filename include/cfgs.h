@@ -1,0 +1,204 @@
+/*
+ * cfgs.h — C ABI of the GB300 (sm_103a) differentiable Gaussian rasteriser.
+ *
+ * This library is a drop-in for the native half of the `diff_gaussian_rasterization`
+ * package that CF-3DGS calls at
+ *   scene/gaussian_model_cf.py:811-882   (CF3DGS_Render.render)
+ *   gaussian_renderer/__init__.py:38-96  (render)
+ *   scene/gaussian_model.py:915-980      (GS_Render.render)
+ * The upstream native module (`diff_gaussian_rasterization._C`, un-vendored in the
+ * reference tree, .gitmodules:4-6) exposes `rasterize_gaussians`,
+ * `rasterize_gaussians_backward` and `mark_visible`; the entry points below replace
+ * those three and add the pose-gradient kernels of the CF-3DGS pose solve
+ * (scene/gaussian_model_cf.py:123-133, trainer/cf3dgs_trainer.py:261-285).
+ *
+ * Conventions
+ *  - Every pointer is a DEVICE pointer unless its comment says "host".
+ *  - The caller owns every buffer. The library allocates nothing and frees nothing;
+ *    the *_bytes() functions size the workspaces.
+ *  - `stream` is a cudaStream_t (0 = legacy default stream). All work is enqueued on
+ *    it; no entry point synchronises unless CfgsSettings.debug is set, except
+ *    cfgs_read_counts(), whose job is to read a device value back.
+ *  - Every entry point returns a CfgsStatus; nonzero means nothing useful was written.
+ *  - Matrices are the 4x4 float tensors CF-3DGS stores on its Camera
+ *    (scene/cameras.py:57-74): row-major storage of the TRANSPOSED matrix, i.e. a
+ *    point p maps to [p,1] @ M (row-vector convention).
+ */
+#ifndef CFGS_H
+#define CFGS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum CfgsStatus {
+  CFGS_OK = 0,
+  CFGS_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size, bad SH degree ...            */
+  CFGS_ERR_CAPACITY = 2,         /* more tile instances than the binning capacity        */
+  CFGS_ERR_LAUNCH = 3,           /* a CUDA launch or runtime call failed                 */
+  CFGS_ERR_DEVICE_FLAG = 4,      /* a kernel raised a flag (see CfgsCounts.flags)        */
+  CFGS_ERR_TOO_LARGE = 5         /* a size above a documented maximum                    */
+} CfgsStatus;
+
+/* Bits of CfgsCounts.flags (raised by kernels, read back with cfgs_read_counts). */
+#define CFGS_FLAG_FRUSTUM_VIOLATION 0x1u /* prefiltered=1 but a point was at view z <= 0.2 */
+#define CFGS_FLAG_CAPACITY_OVERFLOW 0x2u /* K > binning capacity; outputs are invalid      */
+
+/* Tile size of the screen-space binning (pixels). */
+#define CFGS_TILE_X 16
+#define CFGS_TILE_Y 16
+
+/* GaussianRasterizationSettings (NamedTuple, 12 fields, order of
+ * scene/gaussian_model_cf.py:811-824). Tensor fields are device pointers. */
+typedef struct CfgsSettings {
+  int32_t image_height;
+  int32_t image_width;
+  float tanfovx;
+  float tanfovy;
+  const float* bg;          /* [3]  background colour                               */
+  float scale_modifier;
+  const float* viewmatrix;  /* [16] world_view_transform                            */
+  const float* projmatrix;  /* [16] full_proj_transform                             */
+  int32_t sh_degree;        /* active SH degree, 0..3                               */
+  const float* campos;      /* [3]  camera centre                                   */
+  int32_t prefiltered;
+  int32_t debug;            /* 1: synchronise and check after every kernel         */
+} CfgsSettings;
+
+/* The per-Gaussian inputs of GaussianRasterizer.forward. Exactly one of
+ * {shs, colors_precomp} and exactly one of {(scales, rotations), cov3D_precomp}
+ * must be non-null (the Python layer raises before calling otherwise). */
+typedef struct CfgsGaussians {
+  int32_t num_gaussians;       /* N                                                */
+  const float* means3D;        /* [N,3]                                            */
+  const float* opacities;      /* [N]   (already sigmoid-activated)                */
+  const float* shs;            /* [N,M,3] coefficient-major, channel last, or NULL */
+  int32_t sh_coeffs;           /* M = shs.shape[1] (>= (sh_degree+1)^2)            */
+  const float* colors_precomp; /* [N,3] or NULL                                    */
+  const float* scales;         /* [N,3] or NULL (already exp-activated)            */
+  const float* rotations;      /* [N,4] quaternion (r,x,y,z), or NULL              */
+  const float* cov3D_precomp;  /* [N,6] (xx,xy,xz,yy,yz,zz), or NULL               */
+} CfgsGaussians;
+
+/* Gradient outputs of the backward pass (the 8 tensors upstream returns, in its
+ * order). Every non-null array is fully overwritten (zeros for culled Gaussians). */
+typedef struct CfgsGradients {
+  float* dL_dmeans2D;   /* [N,3] d/d(NDC x, NDC y), third column 0             */
+  float* dL_dcolors;    /* [N,3] d/d(per-Gaussian RGB)                        */
+  float* dL_dopacity;   /* [N]                                                */
+  float* dL_dmeans3D;   /* [N,3]                                              */
+  float* dL_dcov3D;     /* [N,6]                                              */
+  float* dL_dsh;        /* [N,M,3] or NULL when colors were precomputed        */
+  float* dL_dscales;    /* [N,3] or NULL when cov3D was precomputed            */
+  float* dL_drotations; /* [N,4] or NULL when cov3D was precomputed            */
+} CfgsGradients;
+
+/* Values the forward leaves in the image workspace; read with cfgs_read_counts(). */
+typedef struct CfgsCounts {
+  uint32_t num_rendered; /* K = total (Gaussian, tile) instances                 */
+  uint32_t flags;        /* CFGS_FLAG_* bits                                     */
+} CfgsCounts;
+
+/* ---- workspace sizing (host functions, no device work) ---------------------- */
+
+/* Per-Gaussian workspace ("geomBuffer" upstream). */
+size_t cfgs_geom_bytes(int32_t num_gaussians);
+/* Per-image workspace ("imageBuffer" upstream): counts, tile ranges, T_final,
+ * contributor counts. */
+size_t cfgs_image_bytes(int32_t image_width, int32_t image_height);
+/* Per-instance workspace ("binningBuffer" upstream) for up to `capacity` instances. */
+size_t cfgs_binning_bytes(int64_t capacity);
+/* Scratch used by cfgs_backward for up to `capacity` instances. */
+size_t cfgs_backward_scratch_bytes(int64_t capacity);
+
+/* Byte offsets of the arrays inside the workspaces, for inspection (tests, debugging;
+ * upstream exposes the same buffers as opaque uint8 tensors).
+ * geom  (10): xy float2, conic_op float4 (a,b,c,opacity), rgbd float4 (r,g,b,depth),
+ *             rect uint2 (x0|y0<<16, x1|y1<<16), touched u32, offset u32, clamped u8,
+ *             block_sums u32, block_prefix u32, total bytes
+ * image (7):  counts CfgsCounts, tile_count u32, tile_range u32[T+1], tile_cursor u32,
+ *             final_T f32, n_contrib u32, total bytes
+ * binning (6): keys u64, keys_alt u64, inst_gid u32, sorted_gid u32, sorted_pidx u32,
+ *             total bytes */
+void cfgs_geom_layout(int32_t num_gaussians, size_t offsets[10]);
+void cfgs_image_layout(int32_t image_width, int32_t image_height, size_t offsets[7]);
+void cfgs_binning_layout(int64_t capacity, size_t offsets[6]);
+
+/* ---- rasteriser forward, phase 1 ---------------------------------------------
+ * Replaces the first half of upstream rasterize_gaussians (markVisible/preprocess
+ * /InclusiveSum): projects every Gaussian (EWA), evaluates SH colour, computes the
+ * screen radius and tile rectangle, counts instances per tile and scans them.
+ * Writes radii[N] (0 = culled) and K into the image workspace. */
+int cfgs_preprocess_forward(const CfgsSettings* settings, const CfgsGaussians* gaussians,
+                            void* geom, void* image, int32_t* radii, void* stream);
+
+/* Copies the CfgsCounts of an image workspace to host memory and synchronises
+ * `stream`. (Upstream reads num_rendered back the same way.) */
+int cfgs_read_counts(const void* image, CfgsCounts* counts_host, void* stream);
+
+/* ---- rasteriser forward, phase 2 ---------------------------------------------
+ * Replaces duplicateWithKeys / SortPairs / identifyTileRanges / render: emits the
+ * K (tile, depth) instances, sorts them per tile by (view depth, instance index) —
+ * the order a stable sort of upstream's 64-bit key (tile << 32 | depth bits) gives —
+ * and alpha-composites every 16x16 tile front to back.
+ * out_color [3,H,W], out_depth [1,H,W], out_alpha [1,H,W]. `capacity` is the number
+ * of instances the binning workspace holds; the device K is used, and if it exceeds
+ * `capacity` the kernels raise CFGS_FLAG_CAPACITY_OVERFLOW and write nothing past it. */
+int cfgs_render_forward(const CfgsSettings* settings, const CfgsGaussians* gaussians,
+                        void* geom, void* image, void* binning, int64_t capacity,
+                        float* out_color, float* out_depth, float* out_alpha, void* stream);
+
+/* ---- rasteriser backward ------------------------------------------------------
+ * Replaces upstream rasterize_gaussians_backward (render backward, computeCov2D
+ * backward, preprocess backward). dL_dcolor [3,H,W]; dL_ddepth and dL_dalpha
+ * [1,H,W] may be NULL (treated as zero). Per-pixel gradients are reduced per
+ * (Gaussian, tile) inside each tile, written once per instance to `scratch`, and
+ * summed per Gaussian in a fixed order: the result is deterministic. */
+int cfgs_backward(const CfgsSettings* settings, const CfgsGaussians* gaussians,
+                  const int32_t* radii, const void* geom, const void* image,
+                  const void* binning, int64_t capacity, void* scratch,
+                  const float* dL_dcolor, const float* dL_ddepth, const float* dL_dalpha,
+                  const CfgsGradients* grads, void* stream);
+
+/* ---- markVisible ---------------------------------------------------------------
+ * Replaces upstream mark_visible (GaussianRasterizer.markVisible): visible[i] = 1
+ * when the point's view-space z > 0.2. */
+int cfgs_mark_visible(int32_t num_points, const float* means3D, const float* viewmatrix,
+                      const float* projmatrix, uint8_t* visible, void* stream);
+
+/* ---- CF-3DGS pose path --------------------------------------------------------
+ * The pose is a tangent vector xi = (rho[3], phi[3]) retracted as exp(xi) * I, the
+ * parametrisation of lietorch's LieGroupParameter(SE3) used by CFGaussianModel.init_RT
+ * (scene/gaussian_model_cf.py:328-340); positions move as exp(xi).act(xyz)
+ * (scene/gaussian_model_cf.py:123-133).
+ *
+ * cfgs_pose_apply: means_out[i] = R(xi) xyz[i] + t(xi); when cov_in/cov_out are
+ * non-null also cov_out[i] = R cov_in[i] R^T (the rotate_cov form). */
+int cfgs_pose_apply(int32_t num_points, const float* xi, const float* xyz,
+                    const float* cov_in, float* means_out, float* cov_out, void* stream);
+
+/* cfgs_pose_grad: dL/dxi [6] from dL/dmeans [N,3] (and, when both are non-null,
+ * dL/dcov [N,6] of the rotated covariances cov_rot [N,6]) without materialising
+ * per-Gaussian Jacobians: one pass forms the 6 (or 6+3) sums, the last block
+ * folds them in a fixed order and applies the SE(3) left-Jacobian transpose.
+ * `scratch` must hold cfgs_pose_scratch_bytes(N) bytes; `grad_out` is [6]. */
+size_t cfgs_pose_scratch_bytes(int32_t num_points);
+int cfgs_pose_grad(int32_t num_points, const float* xi, const float* xyz,
+                   const float* dL_dmeans, const float* cov_rot, const float* dL_dcov,
+                   void* scratch, float* grad_out, void* stream);
+
+/* cfgs_pose_adam: one torch.optim.Adam step (no weight decay, no amsgrad) on the
+ * 6-vector xi, in place, with the step count kept on the device:
+ * state = [m(6), v(6), step(1)] floats. Mirrors the optimiser the reference builds in
+ * training_setup_fix_position (scene/gaussian_model_cf.py:303-326). */
+int cfgs_pose_adam(float* xi, const float* grad, float* state, float lr, float beta1,
+                   float beta2, float eps, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CFGS_H */
