@@ -1,0 +1,360 @@
+#!/usr/bin/env python
+"""Benchmark of the rasteriser hot path: forward + L1 loss + backward of 1,000,000 SH
+degree-3 Gaussians at 1920x1080 (synthetic scene with the workload's shapes and value
+distributions; the reference's datasets are not available).
+
+`python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]`
+prints one JSON line. N > 1 runs N independent replicas under torchrun (the path does
+not shard: no collective), value = total iterations/s over all ranks.
+
+--impl reference times the reference algorithm's CPU implementation (the oracle port,
+C + OpenMP on every host core) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "cf-3dgs_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "fwd+bwd iters/s at 1M Gaussians 1080p"
+UNIT = "iters/s"
+KERNELS_PER_STEP = 7  # preprocess, scan, scatter, tile sort, composite, render bwd, preprocess bwd
+
+
+def _args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=1_000_000)
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-budget-s", type=float, default=20.0)
+    return p.parse_args()
+
+
+def _cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes per launch of each phase
+# ---------------------------------------------------------------------------
+def phase_bytes(N: int, K: int, HW: int, D: int) -> dict:
+    params = N * (12 + 4 + 12 * D + 12 + 16)
+    return {
+        "preprocess": params + N * (8 + 16 + 16 + 8 + 4 + 1 + 4),
+        "bin": N * (4 + 8 + 4 + 4) + K * (8 + 4) + K * (8 + 4 + 8),
+        "composite": K * (4 + 8 + 16 + 16) + HW * (12 + 4 + 4 + 4 + 4),
+        "render_bwd": K * (4 + 4 + 8 + 16 + 16 + 48) + HW * (4 + 4 + 12 + 4 + 4),
+        "preprocess_bwd": params + N * (4 + 4 + 1 + 4) + K * 48 + N * (12 + 12 + 4 + 12 + 24 + 12 * D + 12 + 16),
+    }
+
+
+def _peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def _traffic(kernel: str, K: int):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, scaled to this
+    launch by instance count when the capture was taken on a smaller case."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        e = d[kernel]
+        return e["bytes_per_launch"] * (K / e["num_rendered"]) if e.get("scale_by_instances") else e["bytes_per_launch"]
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(a) -> None:
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    import diff_gaussian_rasterization as dgr
+    from cfgs import raster, scenes
+
+    sc = scenes.scene_large(n=a.n, width=a.width, height=a.height, seed=1)
+    cam = sc.camera.to(dev)
+    rs = dgr.GaussianRasterizationSettings(cam.height, cam.width, cam.tanfovx, cam.tanfovy, sc.bg.to(dev), 1.0,
+                                           cam.viewmatrix, cam.projmatrix, sc.sh_degree, cam.campos, False, False)
+    s = sc.to(dev)
+    target = s.target
+    HW = cam.width * cam.height
+
+    def step(timers=None):
+        color, radii, depth, alpha, st = raster.forward(rs, s.means3D, s.opacities, s.shs, None, s.scales,
+                                                        s.rotations, None, timers=timers)
+        c = color.clamp(0, 1)
+        diff = c - target
+        loss = diff.abs().mean()
+        inside = ((color >= 0) & (color <= 1)).float()
+        g = torch.sign(diff) * inside / color.numel()
+        raster.backward(rs, st, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None, g, None, None,
+                        timers=timers)
+        return loss, st.num_rendered
+
+    for _ in range(max(a.warmup, 0)):
+        step()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    timers: dict = {}
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    t0.record()
+    K = 0
+    for _ in range(a.steps):
+        _, K = step(timers)
+    t1.record()
+    barrier()
+    clk = clocks.stop()
+    total_ms = t0.elapsed_time(t1)
+    if world > 1:
+        tt = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_per_step = total_ms / a.steps
+    value = world * a.steps / (total_ms / 1000.0)
+
+    phase_ms = {k: sum(s_.elapsed_time(e_) for s_, e_ in v) / len(v) for k, v in timers.items()}
+    D = (sc.sh_degree + 1) ** 2
+    pb = phase_bytes(sc.n, K, HW, D)
+    dom = max(phase_ms, key=phase_ms.get)
+    peaks = _peaks()
+    achieved = pb[dom] / (phase_ms[dom] / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 5),
+                "peak_source": peaks["source"], "traffic": _traffic(dom, K),
+                "algorithmic_bytes_per_launch": pb[dom]}
+    phases = {k: {"ms": round(v, 4), "share": round(v / sum(phase_ms.values()), 4),
+                  "hbm_frac": round(pb[k] / (v / 1000.0) / 1e9 / peaks["hbm_gbs"], 5)} for k, v in phase_ms.items()}
+
+    e2e = None
+    if not a.no_e2e:
+        e2e = run_e2e(a, dgr, sc, rs, dev, barrier, world)
+
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        cpu = run_cpu_baseline(sc, a.cpu_budget_s)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{sc.n} SH{sc.sh_degree} Gaussians, {a.width}x{a.height}, "
+                                   f"fwd + L1 loss + bwd", "num_rendered": int(K),
+                       "l2": "inputs larger than L2 (Gaussian parameters "
+                             f"{sc.n * (44 + 12 * D) / 1e6:.0f} MB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "roofline": roofline, "phases": phases, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": KERNELS_PER_STEP * a.steps,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_e2e(a, dgr, sc, rs, dev, barrier, world) -> dict:
+    """Same metric through the public API (GaussianRasterizer + autograd), inputs copied
+    from pinned host memory and the loss read back every step."""
+    import torch
+    host = {k: getattr(sc, k).pin_memory() for k in ("means3D", "opacities", "shs", "scales", "rotations", "target")}
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    raster_mod = dgr.GaussianRasterizer(rs)
+
+    def step():
+        d = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
+        means3D = d["means3D"].requires_grad_(True)
+        means2D = torch.zeros_like(means3D, requires_grad=True)
+        shs = d["shs"].requires_grad_(True)
+        opac = d["opacities"].requires_grad_(True)
+        scales = d["scales"].requires_grad_(True)
+        rots = d["rotations"].requires_grad_(True)
+        color, radii, depth, alpha = raster_mod(means3D=means3D, means2D=means2D, opacities=opac, shs=shs,
+                                                scales=scales, rotations=rots)
+        loss = (color.clamp(0, 1) - d["target"]).abs().mean()
+        loss.backward()
+        return float(loss.item())
+
+    steps = max(3, a.steps // 2)
+    for _ in range(max(a.warmup, 1)):
+        step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    barrier()
+    dt = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([dt], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dt = float(tt.item())
+    return {"value": round(world * steps / dt, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": 4, "steps": steps, "api": "diff_gaussian_rasterization.GaussianRasterizer"}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle: the reported CPU baseline and the --impl reference arm
+# ---------------------------------------------------------------------------
+def _oracle_iteration(sc, Oracle):
+    import numpy as np
+    o = Oracle.from_scene(sc).forward()
+    c = o.color
+    diff = np.clip(c, 0, 1) - sc.target.numpy()
+    g = (np.sign(diff) * ((c >= 0) & (c <= 1))).astype(np.float32) / c.size
+    o.backward(g)
+    return o.K
+
+
+def run_cpu_baseline(sc, budget_s: float) -> dict:
+    from oracle import c_oracle
+    cores = _cores()
+    c_oracle.set_threads(cores)
+    times = []
+    t_start = time.perf_counter()
+    while True:
+        t0 = time.perf_counter()
+        _oracle_iteration(sc, c_oracle.Oracle)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start + times[-1] > budget_s or len(times) >= 5:
+            break
+    t = statistics.median(times)
+    return {"value": round(1.0 / t, 5), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{len(times)} full fwd+bwd iteration(s) of the same workload, median {t:.2f} s"}
+
+
+def run_reference(a) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from cfgs import scenes
+    from oracle import c_oracle
+    cores = _cores()
+    c_oracle.set_threads(cores)
+    sc = scenes.scene_large(n=a.n, width=a.width, height=a.height, seed=1)
+    for _ in range(max(a.warmup, 0)):
+        _oracle_iteration(sc, c_oracle.Oracle)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        _oracle_iteration(sc, c_oracle.Oracle)
+    dt = time.perf_counter() - t0
+    value = a.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1000 * dt / a.steps, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{sc.n} SH{sc.sh_degree} Gaussians, {a.width}x{a.height}, fwd + L1 loss + bwd"},
+        "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"each step one full fwd+bwd iteration ({a.steps} steps)"},
+        "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference rasteriser is CUDA-only and its source is not in the reference tree; this arm "
+                "times the CPU restatement of its algorithm (oracle port) on all host cores",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = _args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -89,6 +89,13 @@ EXPORTS = {
                                       _vp, _vp, _vp, _vp]),
     "cfgs_backward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, _vp, C.c_int64, _vp,
                                 _vp, _vp, _vp, C.POINTER(Gradients), _vp]),
+    "cfgs_bin_forward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, C.c_int64, _vp]),
+    "cfgs_composite_forward": (C.c_int, [C.POINTER(Settings), C.c_int32, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp,
+                                         _vp]),
+    "cfgs_render_backward": (C.c_int, [C.POINTER(Settings), C.c_int32, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp,
+                                       _vp]),
+    "cfgs_preprocess_backward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, C.c_int64, _vp,
+                                           C.POINTER(Gradients), _vp]),
     "cfgs_mark_visible": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_pose_apply": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_pose_scratch_bytes": (C.c_size_t, [C.c_int32]),

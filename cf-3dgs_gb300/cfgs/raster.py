@@ -87,7 +87,25 @@ class ForwardState:
     radii: torch.Tensor
 
 
-def forward(rs, means3D, opacities, shs, colors_precomp, scales, rotations, cov3D_precomp):
+class _Timed:
+    """Brackets one library call with CUDA events on the current stream when `timers`
+    (a dict phase -> list of (start, stop) events) is given."""
+
+    def __init__(self, timers, name):
+        self.timers, self.name = timers, name
+
+    def __enter__(self):
+        if self.timers is not None:
+            self.ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            self.ev[0].record()
+
+    def __exit__(self, *exc):
+        if self.timers is not None:
+            self.ev[1].record()
+            self.timers.setdefault(self.name, []).append(self.ev)
+
+
+def forward(rs, means3D, opacities, shs, colors_precomp, scales, rotations, cov3D_precomp, timers=None):
     """Runs both forward phases. Returns (color, radii, depth, alpha, ForwardState)."""
     lib = native.load()
     dev = means3D.device
@@ -102,8 +120,9 @@ def forward(rs, means3D, opacities, shs, colors_precomp, scales, rotations, cov3
     geom = torch.empty(lib.cfgs_geom_bytes(N), dtype=torch.uint8, device=dev)
     image = torch.empty(lib.cfgs_image_bytes(W, H), dtype=torch.uint8, device=dev)
     radii = torch.empty(N, dtype=torch.int32, device=dev)
-    native.check(lib.cfgs_preprocess_forward(C.byref(s), C.byref(g), geom.data_ptr(), image.data_ptr(),
-                                             radii.data_ptr() if N else None, st), "cfgs_preprocess_forward")
+    with _Timed(timers, "preprocess"):
+        native.check(lib.cfgs_preprocess_forward(C.byref(s), C.byref(g), geom.data_ptr(), image.data_ptr(),
+                                                 radii.data_ptr() if N else None, st), "cfgs_preprocess_forward")
     counts = native.Counts()
     native.check(lib.cfgs_read_counts(image.data_ptr(), C.byref(counts), st), "cfgs_read_counts")
     if counts.flags & native.FLAG_FRUSTUM_VIOLATION:
@@ -115,14 +134,18 @@ def forward(rs, means3D, opacities, shs, colors_precomp, scales, rotations, cov3
     color = torch.empty((3, H, W), dtype=torch.float32, device=dev)
     depth = torch.empty((1, H, W), dtype=torch.float32, device=dev)
     alpha = torch.empty((1, H, W), dtype=torch.float32, device=dev)
-    native.check(lib.cfgs_render_forward(C.byref(s), C.byref(g), geom.data_ptr(), image.data_ptr(),
-                                         binning.data_ptr(), K, color.data_ptr(), depth.data_ptr(),
-                                         alpha.data_ptr(), st), "cfgs_render_forward")
+    with _Timed(timers, "bin"):
+        native.check(lib.cfgs_bin_forward(C.byref(s), C.byref(g), geom.data_ptr(), image.data_ptr(),
+                                          binning.data_ptr(), K, st), "cfgs_bin_forward")
+    with _Timed(timers, "composite"):
+        native.check(lib.cfgs_composite_forward(C.byref(s), N, geom.data_ptr(), image.data_ptr(), binning.data_ptr(),
+                                                K, color.data_ptr(), depth.data_ptr(), alpha.data_ptr(), st),
+                     "cfgs_composite_forward")
     return color, radii, depth, alpha, ForwardState(geom, image, binning, K, radii)
 
 
 def backward(rs, state: ForwardState, means3D, opacities, shs, colors_precomp, scales, rotations,
-             cov3D_precomp, grad_color, grad_depth, grad_alpha):
+             cov3D_precomp, grad_color, grad_depth, grad_alpha, timers=None):
     """Returns (dmeans2D, dcolors, dopacity, dmeans3D, dcov3D, dsh, dscales, drotations)."""
     lib = native.load()
     dev = means3D.device
@@ -155,10 +178,16 @@ def backward(rs, state: ForwardState, means3D, opacities, shs, colors_precomp, s
     gr.dL_dscales = _ptr(d_sc)
     gr.dL_drotations = _ptr(d_rot)
     if N > 0:
-        native.check(lib.cfgs_backward(C.byref(s), C.byref(g), state.radii.data_ptr(), state.geom.data_ptr(),
-                                       state.image.data_ptr(), state.binning.data_ptr(), K, scratch.data_ptr(),
-                                       grad_color.data_ptr(), _ptr(grad_depth), _ptr(grad_alpha), C.byref(gr), st),
-                     "cfgs_backward")
+        with _Timed(timers, "render_bwd"):
+            native.check(lib.cfgs_render_backward(C.byref(s), N, state.geom.data_ptr(), state.image.data_ptr(),
+                                                  state.binning.data_ptr(), K, scratch.data_ptr(),
+                                                  grad_color.data_ptr(), _ptr(grad_depth), _ptr(grad_alpha), st),
+                         "cfgs_render_backward")
+        with _Timed(timers, "preprocess_bwd"):
+            native.check(lib.cfgs_preprocess_backward(C.byref(s), C.byref(g), state.radii.data_ptr(),
+                                                      state.geom.data_ptr(), state.image.data_ptr(), K,
+                                                      scratch.data_ptr(), C.byref(gr), st),
+                         "cfgs_preprocess_backward")
     return d_m2, d_col, d_op, d_m3, d_cov, d_sh, d_sc, d_rot
 
 

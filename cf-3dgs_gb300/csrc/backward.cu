@@ -499,28 +499,18 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(PreBwdArgs a) {
 
 using namespace cfgs;
 
-extern "C" int cfgs_backward(const CfgsSettings* s, const CfgsGaussians* g, const int32_t* radii,
-                             const void* geom, const void* image, const void* binning, int64_t capacity,
-                             void* scratch, const float* dL_dcolor, const float* dL_ddepth,
-                             const float* dL_dalpha, const CfgsGradients* out, void* stream) {
-  if (!s || !g || !geom || !image || !binning || !scratch || !dL_dcolor || !out || !s->bg)
+extern "C" int cfgs_render_backward(const CfgsSettings* s, int32_t num_gaussians, const void* geom, const void* image,
+                                    const void* binning, int64_t capacity, void* scratch, const float* dL_dcolor,
+                                    const float* dL_ddepth, const float* dL_dalpha, void* stream) {
+  if (!s || !geom || !image || !binning || !scratch || !dL_dcolor || !s->bg || num_gaussians < 0)
     return CFGS_ERR_INVALID_ARGUMENT;
-  if (g->num_gaussians == 0) return CFGS_OK;
-  if (g->num_gaussians < 0 || !radii || !g->means3D || !g->opacities) return CFGS_ERR_INVALID_ARGUMENT;
-  if (!out->dL_dmeans2D || !out->dL_dcolors || !out->dL_dopacity || !out->dL_dmeans3D || !out->dL_dcov3D)
-    return CFGS_ERR_INVALID_ARGUMENT;
-  if (!g->cov3D_precomp && (!out->dL_dscales || !out->dL_drotations || !g->scales || !g->rotations))
-    return CFGS_ERR_INVALID_ARGUMENT;
-  if ((g->shs == nullptr) == (g->colors_precomp == nullptr)) return CFGS_ERR_INVALID_ARGUMENT;
-  if (g->shs && !s->campos) return CFGS_ERR_INVALID_ARGUMENT;
+  if (s->image_width <= 0 || s->image_height <= 0) return CFGS_ERR_INVALID_ARGUMENT;
   if (capacity < 0 || capacity > 0x7fffffffll) return CFGS_ERR_INVALID_ARGUMENT;
   cudaStream_t st = (cudaStream_t)stream;
   ImageLayout IL(s->image_width, s->image_height);
   ImageView iv(const_cast<void*>(image), s->image_width, s->image_height);
-  GeomView gv(const_cast<void*>(geom), g->num_gaussians);
+  GeomView gv(const_cast<void*>(geom), num_gaussians);
   BinningView bv(const_cast<void*>(binning), capacity);
-  float4* records = static_cast<float4*>(scratch);
-
   RenderBwdArgs ra;
   ra.W = s->image_width;
   ra.H = s->image_height;
@@ -537,25 +527,54 @@ extern "C" int cfgs_backward(const CfgsSettings* s, const CfgsGaussians* g, cons
   ra.dL_dcolor = dL_dcolor;
   ra.dL_ddepth = dL_ddepth;
   ra.dL_dalpha = dL_dalpha;
-  ra.records = records;
+  ra.records = static_cast<float4*>(scratch);
   ra.cap = capacity;
   ra.counts = iv.counts;
   k_render_bwd<<<IL.num_tiles, kTilePixels, 0, st>>>(ra);
   CFGS_CHECK_LAUNCH(s->debug, st);
-  if (g->num_gaussians > 0) {
-    PreBwdArgs pa;
-    pa.s = *s;
-    pa.g = *g;
-    pa.radii = radii;
-    pa.geom = gv;
-    pa.records = records;
-    pa.out = *out;
-    pa.focal_x = (float)s->image_width / (2.0f * s->tanfovx);
-    pa.focal_y = (float)s->image_height / (2.0f * s->tanfovy);
-    pa.cap = capacity;
-    pa.counts = iv.counts;
-    k_preprocess_bwd<<<div_up(g->num_gaussians, 256), 256, 0, st>>>(pa);
-    CFGS_CHECK_LAUNCH(s->debug, st);
-  }
   return CFGS_OK;
+}
+
+extern "C" int cfgs_preprocess_backward(const CfgsSettings* s, const CfgsGaussians* g, const int32_t* radii,
+                                        const void* geom, const void* image, int64_t capacity, const void* scratch,
+                                        const CfgsGradients* out, void* stream) {
+  if (!s || !g || !geom || !image || !scratch || !out || !s->viewmatrix || !s->projmatrix)
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if (g->num_gaussians == 0) return CFGS_OK;
+  if (g->num_gaussians < 0 || !radii || !g->means3D || !g->opacities) return CFGS_ERR_INVALID_ARGUMENT;
+  if (!out->dL_dmeans2D || !out->dL_dcolors || !out->dL_dopacity || !out->dL_dmeans3D || !out->dL_dcov3D)
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if (!g->cov3D_precomp && (!out->dL_dscales || !out->dL_drotations || !g->scales || !g->rotations))
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if ((g->shs == nullptr) == (g->colors_precomp == nullptr)) return CFGS_ERR_INVALID_ARGUMENT;
+  if (g->shs && !s->campos) return CFGS_ERR_INVALID_ARGUMENT;
+  if (capacity < 0 || capacity > 0x7fffffffll) return CFGS_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  ImageView iv(const_cast<void*>(image), s->image_width, s->image_height);
+  PreBwdArgs pa;
+  pa.s = *s;
+  pa.g = *g;
+  pa.radii = radii;
+  pa.geom = GeomView(const_cast<void*>(geom), g->num_gaussians);
+  pa.records = static_cast<const float4*>(scratch);
+  pa.out = *out;
+  pa.focal_x = (float)s->image_width / (2.0f * s->tanfovx);
+  pa.focal_y = (float)s->image_height / (2.0f * s->tanfovy);
+  pa.cap = capacity;
+  pa.counts = iv.counts;
+  k_preprocess_bwd<<<div_up(g->num_gaussians, 256), 256, 0, st>>>(pa);
+  CFGS_CHECK_LAUNCH(s->debug, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_backward(const CfgsSettings* s, const CfgsGaussians* g, const int32_t* radii, const void* geom,
+                             const void* image, const void* binning, int64_t capacity, void* scratch,
+                             const float* dL_dcolor, const float* dL_ddepth, const float* dL_dalpha,
+                             const CfgsGradients* out, void* stream) {
+  if (!g) return CFGS_ERR_INVALID_ARGUMENT;
+  if (g->num_gaussians == 0) return CFGS_OK;
+  int st = cfgs_render_backward(s, g->num_gaussians, geom, image, binning, capacity, scratch, dL_dcolor, dL_ddepth,
+                                dL_dalpha, stream);
+  if (st != CFGS_OK) return st;
+  return cfgs_preprocess_backward(s, g, radii, geom, image, capacity, scratch, out, stream);
 }

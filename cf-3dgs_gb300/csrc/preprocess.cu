@@ -367,10 +367,10 @@ static bool settings_ok(const CfgsSettings* s) {
 
 extern "C" int cfgs_preprocess_forward(const CfgsSettings* s, const CfgsGaussians* g, void* geom,
                                        void* image, int32_t* radii, void* stream) {
-  if (!settings_ok(s) || !g || !geom || !image || !radii) return CFGS_ERR_INVALID_ARGUMENT;
+  if (!settings_ok(s) || !g || !geom || !image) return CFGS_ERR_INVALID_ARGUMENT;
   if (g->num_gaussians < 0) return CFGS_ERR_INVALID_ARGUMENT;
   if (g->num_gaussians > 0) {
-    if (!g->means3D || !g->opacities) return CFGS_ERR_INVALID_ARGUMENT;
+    if (!g->means3D || !g->opacities || !radii) return CFGS_ERR_INVALID_ARGUMENT;
     if ((g->shs == nullptr) == (g->colors_precomp == nullptr)) return CFGS_ERR_INVALID_ARGUMENT;
     if (g->cov3D_precomp == nullptr && (g->scales == nullptr || g->rotations == nullptr))
       return CFGS_ERR_INVALID_ARGUMENT;

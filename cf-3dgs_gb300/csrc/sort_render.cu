@@ -276,11 +276,9 @@ __global__ void __launch_bounds__(kTilePixels) k_render_fwd(RenderArgs a) {
 
 using namespace cfgs;
 
-extern "C" int cfgs_render_forward(const CfgsSettings* s, const CfgsGaussians* g, void* geom, void* image,
-                                   void* binning, int64_t capacity, float* out_color, float* out_depth,
-                                   float* out_alpha, void* stream) {
-  if (!s || !g || !geom || !image || !binning || !out_color || capacity < 0 || !s->bg)
-    return CFGS_ERR_INVALID_ARGUMENT;
+extern "C" int cfgs_bin_forward(const CfgsSettings* s, const CfgsGaussians* g, void* geom, void* image, void* binning,
+                                int64_t capacity, void* stream) {
+  if (!s || !g || !geom || !image || !binning || capacity < 0) return CFGS_ERR_INVALID_ARGUMENT;
   if (s->image_width <= 0 || s->image_height <= 0 || g->num_gaussians < 0) return CFGS_ERR_INVALID_ARGUMENT;
   if (capacity > 0x7fffffffll) return CFGS_ERR_TOO_LARGE;
   cudaStream_t st = (cudaStream_t)stream;
@@ -297,6 +295,21 @@ extern "C" int cfgs_render_forward(const CfgsSettings* s, const CfgsGaussians* g
   SortArgs so{iv.tile_range, bv, capacity, iv.counts};
   k_tile_sort<<<IL.num_tiles, kSortThreads, 0, st>>>(so);
   CFGS_CHECK_LAUNCH(s->debug, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_composite_forward(const CfgsSettings* s, int32_t num_gaussians, const void* geom, const void* image,
+                                      const void* binning, int64_t capacity, float* out_color, float* out_depth,
+                                      float* out_alpha, void* stream) {
+  if (!s || !geom || !image || !binning || !out_color || capacity < 0 || !s->bg || num_gaussians < 0)
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if (s->image_width <= 0 || s->image_height <= 0) return CFGS_ERR_INVALID_ARGUMENT;
+  if (capacity > 0x7fffffffll) return CFGS_ERR_TOO_LARGE;
+  cudaStream_t st = (cudaStream_t)stream;
+  ImageLayout IL(s->image_width, s->image_height);
+  ImageView iv(const_cast<void*>(image), s->image_width, s->image_height);
+  GeomView gv(const_cast<void*>(geom), num_gaussians);
+  BinningView bv(const_cast<void*>(binning), capacity);
   RenderArgs ra;
   ra.W = s->image_width;
   ra.H = s->image_height;
@@ -317,4 +330,13 @@ extern "C" int cfgs_render_forward(const CfgsSettings* s, const CfgsGaussians* g
   k_render_fwd<<<IL.num_tiles, kTilePixels, 0, st>>>(ra);
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;
+}
+
+extern "C" int cfgs_render_forward(const CfgsSettings* s, const CfgsGaussians* g, void* geom, void* image,
+                                   void* binning, int64_t capacity, float* out_color, float* out_depth,
+                                   float* out_alpha, void* stream) {
+  int st = cfgs_bin_forward(s, g, geom, image, binning, capacity, stream);
+  if (st != CFGS_OK) return st;
+  return cfgs_composite_forward(s, g->num_gaussians, geom, image, binning, capacity, out_color, out_depth, out_alpha,
+                                stream);
 }

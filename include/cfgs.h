@@ -151,6 +151,15 @@ int cfgs_render_forward(const CfgsSettings* settings, const CfgsGaussians* gauss
                         void* geom, void* image, void* binning, int64_t capacity,
                         float* out_color, float* out_depth, float* out_alpha, void* stream);
 
+/* The two halves of cfgs_render_forward, for callers that time or schedule them
+ * separately: instance emission + per-tile sort (duplicateWithKeys / SortPairs /
+ * identifyTileRanges upstream), then compositing (renderCUDA upstream). */
+int cfgs_bin_forward(const CfgsSettings* settings, const CfgsGaussians* gaussians, void* geom, void* image,
+                     void* binning, int64_t capacity, void* stream);
+int cfgs_composite_forward(const CfgsSettings* settings, int32_t num_gaussians, const void* geom,
+                           const void* image, const void* binning, int64_t capacity, float* out_color,
+                           float* out_depth, float* out_alpha, void* stream);
+
 /* ---- rasteriser backward ------------------------------------------------------
  * Replaces upstream rasterize_gaussians_backward (render backward, computeCov2D
  * backward, preprocess backward). dL_dcolor [3,H,W]; dL_ddepth and dL_dalpha
@@ -162,6 +171,16 @@ int cfgs_backward(const CfgsSettings* settings, const CfgsGaussians* gaussians,
                   const void* binning, int64_t capacity, void* scratch,
                   const float* dL_dcolor, const float* dL_ddepth, const float* dL_dalpha,
                   const CfgsGradients* grads, void* stream);
+
+/* The two halves of cfgs_backward: the per-tile render backward (renderCUDA backward
+ * upstream) writing one record per instance into `scratch`, then the per-Gaussian
+ * preprocess backward (computeCov2DCUDA + preprocessCUDA backward upstream). */
+int cfgs_render_backward(const CfgsSettings* settings, int32_t num_gaussians, const void* geom,
+                         const void* image, const void* binning, int64_t capacity, void* scratch,
+                         const float* dL_dcolor, const float* dL_ddepth, const float* dL_dalpha, void* stream);
+int cfgs_preprocess_backward(const CfgsSettings* settings, const CfgsGaussians* gaussians,
+                             const int32_t* radii, const void* geom, const void* image, int64_t capacity,
+                             const void* scratch, const CfgsGradients* grads, void* stream);
 
 /* ---- markVisible ---------------------------------------------------------------
  * Replaces upstream mark_visible (GaussianRasterizer.markVisible): visible[i] = 1

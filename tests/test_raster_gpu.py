@@ -231,7 +231,7 @@ def test_empty_and_culled(dgr):
     color, radii, depth, alpha, leaves, _ = _run_autograd(dgr, sc)
     assert int(radii.abs().sum()) == 0
     assert torch.equal(color.detach().cpu(), sc.bg[:, None, None].expand(3, 40, 48).contiguous())
-    assert float(alpha.abs().max()) == 0.0
+    assert float(alpha.detach().abs().max()) == 0.0
     assert float(leaves["means3D"].grad.abs().max()) == 0.0
     empty = scenes.scene_small(n=0, width=33, height=17, seed=1)
     color, radii, depth, alpha, state, v = _gpu_forward(dgr, empty)
