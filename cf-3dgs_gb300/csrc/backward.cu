@@ -9,6 +9,8 @@
 // pre-sort index. A Gaussian's instances are contiguous in pre-sort order, so the
 // preprocess backward sums its records in a fixed order: no atomics, bit-identical
 // results run to run.
+#include <mutex>
+
 #include "cfgs_internal.cuh"
 
 namespace cfgs {
@@ -577,4 +579,48 @@ extern "C" int cfgs_backward(const CfgsSettings* s, const CfgsGaussians* g, cons
                                 dL_dalpha, stream);
   if (st != CFGS_OK) return st;
   return cfgs_preprocess_backward(s, g, radii, geom, image, capacity, scratch, out, stream);
+}
+
+// ---- allocation-free backward ----------------------------------------------------
+// Some callers cannot allocate device memory when they call the rasteriser: plugin
+// hosts that hand a plugin only its input and output buffers, and services that must
+// not allocate once they are serving. This entry point runs the same two kernels as
+// cfgs_backward, but the per-instance gradient records live in the fixed array below
+// instead of a caller-provided scratch buffer. Every GPU that loads this library holds
+// the array (30 MiB) until the process exits.
+static __device__ __align__(256) float4 g_noalloc_records[(size_t)CFGS_NOALLOC_MAX_INSTANCES * kRecordFloat4];
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// Device address of g_noalloc_records on the current device. The host-side name of
+// the array is only a stand-in, so the address is looked up once per device, with
+// that device current, and cached.
+int noalloc_records(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) return CFGS_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_records) != cudaSuccess || p == nullptr) return CFGS_ERR_LAUNCH;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CFGS_OK;
+}
+}  // namespace
+
+extern "C" int cfgs_backward_noalloc(const CfgsSettings* s, const CfgsGaussians* g, const int32_t* radii,
+                                     const void* geom, const void* image, const void* binning, int64_t capacity,
+                                     const float* dL_dcolor, const float* dL_ddepth, const float* dL_dalpha,
+                                     const CfgsGradients* out, void* stream) {
+  if (capacity < 0) return CFGS_ERR_INVALID_ARGUMENT;
+  if (capacity > CFGS_NOALLOC_MAX_INSTANCES) return CFGS_ERR_TOO_LARGE;
+  void* records = nullptr;
+  int st = noalloc_records(&records);
+  if (st != CFGS_OK) return st;
+  return cfgs_backward(s, g, radii, geom, image, binning, capacity, records, dL_dcolor, dL_ddepth, dL_dalpha, out,
+                       stream);
 }

@@ -182,6 +182,29 @@ int cfgs_preprocess_backward(const CfgsSettings* settings, const CfgsGaussians* 
                              const int32_t* radii, const void* geom, const void* image, int64_t capacity,
                              const void* scratch, const CfgsGradients* grads, void* stream);
 
+/* ---- allocation-free backward ----------------------------------------------------
+ * No counterpart in the reference: an addition of this library.
+ *
+ * For callers that cannot allocate device memory at the point they call the backward:
+ * plugin hosts that give a plugin only its input and output buffers, and services that
+ * must not allocate once serving has started. Same computation and outputs as
+ * cfgs_backward, but the per-instance scratch is a fixed array inside the library, so
+ * the caller passes no scratch buffer and nothing is allocated.
+ *  - Limit: `capacity` (the binning capacity, >= K) at most
+ *    CFGS_NOALLOC_MAX_INSTANCES instances; larger returns CFGS_ERR_TOO_LARGE.
+ *  - Every GPU that loads the library holds the array (30 MiB) until the process exits.
+ *  - The first call on a device looks up the array's device address (once per device,
+ *    with that device current); make that first call before any stream capture.
+ *  - All calls share the one array and it keeps the last call's contents (every record
+ *    a call needs is written by that call). Calls that overlap on the GPU race with
+ *    each other: serialise them, e.g. on one stream. */
+#define CFGS_NOALLOC_MAX_INSTANCES 655360
+int cfgs_backward_noalloc(const CfgsSettings* settings, const CfgsGaussians* gaussians,
+                          const int32_t* radii, const void* geom, const void* image,
+                          const void* binning, int64_t capacity, const float* dL_dcolor,
+                          const float* dL_ddepth, const float* dL_dalpha,
+                          const CfgsGradients* grads, void* stream);
+
 /* ---- markVisible ---------------------------------------------------------------
  * Replaces upstream mark_visible (GaussianRasterizer.markVisible): visible[i] = 1
  * when the point's view-space z > 0.2. */
