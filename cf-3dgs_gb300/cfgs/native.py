@@ -100,7 +100,7 @@ EXPORTS = {
     "cfgs_pose_apply": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_pose_scratch_bytes": (C.c_size_t, [C.c_int32]),
     "cfgs_pose_grad": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
-    "cfgs_pose_adam": (C.c_int, [_vp, _vp, _vp, C.c_float, C.c_float, C.c_float, C.c_float, _vp]),
+    "cfgs_pose_adam": (C.c_int, [C.c_int32, _vp, _vp, _vp, C.c_double, C.c_double, C.c_double, C.c_double, _vp]),
 }
 
 _LIB = None

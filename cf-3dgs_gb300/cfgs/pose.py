@@ -90,9 +90,33 @@ def pose_error(xi_a: np.ndarray, xi_b: np.ndarray):
     return math.degrees(math.acos(cos)), float(np.linalg.norm(ta - tb))
 
 
+class _Act(torch.autograd.Function):
+    """p' = R p + t for rotations/translations given in float64. Forward: R and t are
+    rounded to the positions' dtype and each position is ((R0 x + R1 y) + R2 z) + t,
+    one rounding per operation (the order the cfgs_pose_apply kernel uses, so both
+    paths place the Gaussians identically). Backward: dL/dR = sum g p^T and
+    dL/dt = sum g, reduced in float64."""
+
+    @staticmethod
+    def forward(ctx, R64, t64, xyz):
+        R, t = R64.to(xyz.dtype), t64.to(xyz.dtype)
+        x, y, z = xyz[:, 0:1], xyz[:, 1:2], xyz[:, 2:3]
+        ctx.save_for_backward(xyz)
+        return ((R[:, 0][None] * x + R[:, 1][None] * y) + R[:, 2][None] * z) + t[None]
+
+    @staticmethod
+    def backward(ctx, g):
+        (xyz,) = ctx.saved_tensors
+        g64 = g.double()
+        return g64.t() @ xyz.double(), g64.sum(0), None
+
+
 def apply_pose_torch(xi: torch.Tensor, xyz: torch.Tensor, cov6: torch.Tensor | None = None):
-    R, t = se3_exp(xi)
-    means = xyz @ R.t() + t
+    """exp(xi).act(xyz) with autograd (the plain path). The exponential and the
+    gradient reductions run in float64; the positions are float32 (see _Act)."""
+    R64, t64 = se3_exp(xi.double())
+    means = _Act.apply(R64, t64, xyz)
+    R = R64.to(xyz.dtype)
     if cov6 is None:
         return means, None
     S = torch.stack([cov6[:, 0], cov6[:, 1], cov6[:, 2], cov6[:, 1], cov6[:, 3], cov6[:, 4], cov6[:, 2],
@@ -158,19 +182,21 @@ def pose_apply(xi, xyz, cov6=None):
 
 
 class FusedAdam:
-    """torch.optim.Adam (no weight decay) on a 6-vector, one kernel per step; the step
-    count and moments stay on the device."""
+    """torch.optim.Adam (no weight decay) on one or more 6-vectors (xi [6] or [S,6]),
+    one kernel per step for all of them; moments and step counts stay on the device."""
 
     def __init__(self, xi: torch.Tensor, lr=1e-3, betas=(0.9, 0.999), eps=1e-15):
         self.xi = xi
-        self.lr, self.b1, self.b2, self.eps = lr, betas[0], betas[1], eps
-        self.state = torch.zeros(13, dtype=torch.float32, device=xi.device)
+        self.count = xi.numel() // 6
+        self.lr, self.b1, self.b2, self.eps = float(lr), float(betas[0]), float(betas[1]), float(eps)
+        self.state = torch.zeros(self.count, 16, dtype=torch.float32, device=xi.device)
 
     def step(self, grad: torch.Tensor):
         lib = native.load()
         st = torch.cuda.current_stream(self.xi.device).cuda_stream
-        native.check(lib.cfgs_pose_adam(self.xi.data_ptr(), grad.contiguous().data_ptr(), self.state.data_ptr(),
-                                        self.lr, self.b1, self.b2, self.eps, st), "cfgs_pose_adam")
+        native.check(lib.cfgs_pose_adam(self.count, self.xi.data_ptr(), grad.contiguous().data_ptr(),
+                                        self.state.data_ptr(), self.lr, self.b1, self.b2, self.eps, st),
+                     "cfgs_pose_adam")
 
 
 # ---------------------------------------------------------------------------
@@ -239,7 +265,7 @@ def solve(prob: PoseProblem, iters: int = 300, lr: float = 1e-3, mode: str = "fu
             opt.step()
             opt.zero_grad(set_to_none=True)
             if record:
-                losses.append(float(loss))
+                losses.append(float(loss.detach()))
         return xi.detach().double().cpu().numpy(), losses
     if mode == "fused":
         xi = torch.zeros(6, dtype=torch.float32, device=dev)
@@ -251,7 +277,7 @@ def solve(prob: PoseProblem, iters: int = 300, lr: float = 1e-3, mode: str = "fu
             loss.backward()
             opt.step(xi_leaf.grad)
             if record:
-                losses.append(float(loss))
+                losses.append(float(loss.detach()))
         return xi.detach().double().cpu().numpy(), losses
     raise ValueError(mode)
 

@@ -121,7 +121,10 @@ __global__ void __launch_bounds__(kPoseThreads) k_pose_apply(int n, const float*
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     float p0 = xyz[3 * i], p1 = xyz[3 * i + 1], p2 = xyz[3 * i + 2];
 #pragma unroll
-    for (int r = 0; r < 3; ++r) means_out[3 * i + r] = R[3 * r] * p0 + R[3 * r + 1] * p1 + R[3 * r + 2] * p2 + st[r];
+    for (int r = 0; r < 3; ++r)  // ((R0 x + R1 y) + R2 z) + t, each operation rounded once
+      means_out[3 * i + r] = __fadd_rn(
+          __fadd_rn(__fadd_rn(__fmul_rn(R[3 * r], p0), __fmul_rn(R[3 * r + 1], p1)), __fmul_rn(R[3 * r + 2], p2)),
+          st[r]);
     if (cov_in) {
       const float* c = cov_in + 6 * (size_t)i;
       float C[9] = {c[0], c[1], c[2], c[1], c[3], c[4], c[2], c[4], c[5]};
@@ -147,34 +150,39 @@ struct PoseGradArgs {
   const float* dL_dmeans;
   const float* cov_rot;
   const float* dL_dcov;
-  float* partials;        // [gridDim.x][9]
+  double* partials;       // [gridDim.x][9]
   unsigned int* counter;  // zeroed before launch
   float* grad_out;        // [6]
 };
 
+// Sums in float64: the per-Gaussian terms (R p) x g use the float64 rotation and
+// exact float32 x float32 products, so the result is the float64 value of the same
+// sums a float64 autograd of exp(xi).act(p) forms; rounded to float32 at the end, the
+// gradient then matches that path's in all but boundary cases, which keeps the fused
+// and plain solves on the same trajectory.
 __global__ void __launch_bounds__(kPoseThreads) k_pose_grad(PoseGradArgs a) {
-  __shared__ float sR[9];
-  __shared__ float s_red[kPoseThreads / 32][kPosePartials];
+  __shared__ double sR[9];
+  __shared__ double s_red[kPoseThreads / 32][kPosePartials];
   __shared__ bool s_last;
   if (threadIdx.x == 0) {
     SE3d X;
     double Jl[9];
     se3_exp(a.xi, &X, Jl);
-    for (int k = 0; k < 9; ++k) sR[k] = (float)X.R[k];
+    for (int k = 0; k < 9; ++k) sR[k] = X.R[k];
   }
   __syncthreads();
-  float R[9];
+  double R[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) R[k] = sR[k];
-  float acc[kPosePartials];
+  double acc[kPosePartials];
 #pragma unroll
-  for (int k = 0; k < kPosePartials; ++k) acc[k] = 0.f;
+  for (int k = 0; k < kPosePartials; ++k) acc[k] = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x) {
-    float p0 = a.xyz[3 * i], p1 = a.xyz[3 * i + 1], p2 = a.xyz[3 * i + 2];
-    float g0 = a.dL_dmeans[3 * i], g1 = a.dL_dmeans[3 * i + 1], g2 = a.dL_dmeans[3 * i + 2];
-    float q0 = R[0] * p0 + R[1] * p1 + R[2] * p2;
-    float q1 = R[3] * p0 + R[4] * p1 + R[5] * p2;
-    float q2 = R[6] * p0 + R[7] * p1 + R[8] * p2;
+    double p0 = a.xyz[3 * i], p1 = a.xyz[3 * i + 1], p2 = a.xyz[3 * i + 2];
+    double g0 = a.dL_dmeans[3 * i], g1 = a.dL_dmeans[3 * i + 1], g2 = a.dL_dmeans[3 * i + 2];
+    double q0 = R[0] * p0 + R[1] * p1 + R[2] * p2;
+    double q1 = R[3] * p0 + R[4] * p1 + R[5] * p2;
+    double q2 = R[6] * p0 + R[7] * p1 + R[8] * p2;
     acc[0] += g0;
     acc[1] += g1;
     acc[2] += g2;
@@ -193,21 +201,21 @@ __global__ void __launch_bounds__(kPoseThreads) k_pose_grad(PoseGradArgs a) {
 #pragma unroll
         for (int s = 0; s < 3; ++s) CG[3 * r + s] = C[3 * r] * G[s] + C[3 * r + 1] * G[3 + s] + C[3 * r + 2] * G[6 + s];
       // (G C) = (C G)^T for symmetric C, G, so M_rs = CG_rs - CG_sr.
-      acc[6] += 2.f * (CG[5] - CG[7]);
-      acc[7] += 2.f * (CG[6] - CG[2]);
-      acc[8] += 2.f * (CG[1] - CG[3]);
+      acc[6] += 2.0 * ((double)CG[5] - (double)CG[7]);
+      acc[7] += 2.0 * ((double)CG[6] - (double)CG[2]);
+      acc[8] += 2.0 * ((double)CG[1] - (double)CG[3]);
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < kPosePartials; ++k) {
-    float v = acc[k];
+    double v = acc[k];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) s_red[warp][k] = v;
   }
   __syncthreads();
   if (threadIdx.x < kPosePartials) {
-    float v = 0.f;
+    double v = 0.0;
     for (int w = 0; w < kPoseThreads / 32; ++w) v += s_red[w][threadIdx.x];
     a.partials[blockIdx.x * kPosePartials + threadIdx.x] = v;
   }
@@ -220,9 +228,9 @@ __global__ void __launch_bounds__(kPoseThreads) k_pose_grad(PoseGradArgs a) {
   if (threadIdx.x == 0) {
     double tot[kPosePartials];
     for (int k = 0; k < kPosePartials; ++k) tot[k] = 0.0;
-    const volatile float* part = a.partials;
+    const volatile double* part = a.partials;
     for (int b = 0; b < (int)gridDim.x; ++b)
-      for (int k = 0; k < kPosePartials; ++k) tot[k] += (double)part[b * kPosePartials + k];
+      for (int k = 0; k < kPosePartials; ++k) tot[k] += part[b * kPosePartials + k];
     SE3d X;
     double Jl[9], Q[9];
     se3_exp(a.xi, &X, Jl);
@@ -245,25 +253,39 @@ __global__ void __launch_bounds__(kPoseThreads) k_pose_grad(PoseGradArgs a) {
   }
 }
 
-// torch.optim.Adam step (single-tensor path) on the 6-vector.
-__global__ void k_pose_adam(float* xi, const float* grad, float* state, float lr, float b1, float b2, float eps) {
-  int k = threadIdx.x;
-  float step = state[12] + 1.0f;
-  if (k < 6) {
-    float g = grad[k];
-    float m = state[k], v = state[6 + k];
-    m = m + (g - m) * (1.0f - b1);
-    v = v * b2 + (1.0f - b2) * g * g;
-    state[k] = m;
-    state[6 + k] = v;
-    double bc1 = 1.0 - pow((double)b1, (double)step);
-    double bc2 = 1.0 - pow((double)b2, (double)step);
-    float step_size = (float)(lr / bc1);
-    float denom = sqrtf(v) / (float)sqrt(bc2) + eps;
-    xi[k] = xi[k] - step_size * (m / denom);
+// One Adam step on `count` 6-vectors (one per solve), following the operation sequence
+// of torch.optim.Adam's default multi-tensor path for float32 CUDA tensors:
+//   m = lerp(m, g, 1 - b1);  v = v * b2;  v = addcmul(v, g, g, 1 - b2);
+//   denom = sqrt(v) / sqrt(1 - b2^t) + eps;  p = addcdiv(p, m, denom, -lr / (1 - b1^t))
+// with the hyper-parameters as float64 scalars rounded to float32 per use, as torch
+// passes them, so both optimisers take the same steps.
+// state per solve: m[6], v[6], step, 3 unused floats.
+__global__ void k_pose_adam(int count, float* xi, const float* grad, float* state, double lr, double b1, double b2,
+                            double eps) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= count) return;
+  float* st = state + 16 * (size_t)s;
+  const float step = st[12] + 1.0f;
+  const float w1 = (float)(1.0 - b1), mul2 = (float)b2, w2 = (float)(1.0 - b2);
+  const double bc1 = 1.0 - pow(b1, (double)step);
+  const double bc2 = 1.0 - pow(b2, (double)step);
+  const float step_size = (float)(-(lr / bc1));
+  const float bc2_sqrt = (float)sqrt(bc2);
+  const float eps_f = (float)eps;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const float g = grad[6 * (size_t)s + k];
+    float m = st[k], v = st[6 + k];
+    m = fmaf(w1, g - m, m);
+    v = v * mul2;
+    v = fmaf(w2, g * g, v);
+    st[k] = m;
+    st[6 + k] = v;
+    float denom = sqrtf(v) / bc2_sqrt;
+    denom = denom + eps_f;
+    xi[6 * (size_t)s + k] = fmaf(step_size, m / denom, xi[6 * (size_t)s + k]);
   }
-  __syncthreads();
-  if (k == 0) state[12] = step;
+  st[12] = step;
 }
 
 }  // namespace cfgs
@@ -287,7 +309,7 @@ extern "C" int cfgs_pose_apply(int32_t n, const float* xi, const float* xyz, con
 
 extern "C" size_t cfgs_pose_scratch_bytes(int32_t n) {
   (void)n;
-  return align256(sizeof(float) * kPosePartials * kPoseMaxBlocks) + 256;
+  return align256(sizeof(double) * kPosePartials * kPoseMaxBlocks) + 256;
 }
 
 extern "C" int cfgs_pose_grad(int32_t n, const float* xi, const float* xyz, const float* dL_dmeans, const float* cov_rot,
@@ -302,9 +324,9 @@ extern "C" int cfgs_pose_grad(int32_t n, const float* xi, const float* xyz, cons
   a.dL_dmeans = dL_dmeans;
   a.cov_rot = cov_rot;
   a.dL_dcov = dL_dcov;
-  a.partials = static_cast<float*>(scratch);
+  a.partials = static_cast<double*>(scratch);
   a.counter = reinterpret_cast<unsigned int*>(static_cast<char*>(scratch) +
-                                              align256(sizeof(float) * kPosePartials * kPoseMaxBlocks));
+                                              align256(sizeof(double) * kPosePartials * kPoseMaxBlocks));
   a.grad_out = grad_out;
   if (cudaMemsetAsync(a.counter, 0, sizeof(unsigned int), st) != cudaSuccess) return CFGS_ERR_LAUNCH;
   k_pose_grad<<<pose_blocks(n), kPoseThreads, 0, st>>>(a);
@@ -312,10 +334,11 @@ extern "C" int cfgs_pose_grad(int32_t n, const float* xi, const float* xyz, cons
   return CFGS_OK;
 }
 
-extern "C" int cfgs_pose_adam(float* xi, const float* grad, float* state, float lr, float beta1, float beta2, float eps,
-                              void* stream) {
-  if (!xi || !grad || !state) return CFGS_ERR_INVALID_ARGUMENT;
-  k_pose_adam<<<1, 32, 0, (cudaStream_t)stream>>>(xi, grad, state, lr, beta1, beta2, eps);
+extern "C" int cfgs_pose_adam(int32_t count, float* xi, const float* grad, float* state, double lr, double beta1,
+                              double beta2, double eps, void* stream) {
+  if (count < 0 || (count > 0 && (!xi || !grad || !state))) return CFGS_ERR_INVALID_ARGUMENT;
+  if (count == 0) return CFGS_OK;
+  k_pose_adam<<<div_up(count, 128), 128, 0, (cudaStream_t)stream>>>(count, xi, grad, state, lr, beta1, beta2, eps);
   CFGS_CHECK_LAUNCH(0, stream);
   return CFGS_OK;
 }

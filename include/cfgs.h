@@ -232,12 +232,15 @@ int cfgs_pose_grad(int32_t num_points, const float* xi, const float* xyz,
                    const float* dL_dmeans, const float* cov_rot, const float* dL_dcov,
                    void* scratch, float* grad_out, void* stream);
 
-/* cfgs_pose_adam: one torch.optim.Adam step (no weight decay, no amsgrad) on the
- * 6-vector xi, in place, with the step count kept on the device:
- * state = [m(6), v(6), step(1)] floats. Mirrors the optimiser the reference builds in
- * training_setup_fix_position (scene/gaussian_model_cf.py:303-326). */
-int cfgs_pose_adam(float* xi, const float* grad, float* state, float lr, float beta1,
-                   float beta2, float eps, void* stream);
+/* cfgs_pose_adam: one torch.optim.Adam step (no weight decay, no amsgrad) on `count`
+ * independent 6-vectors xi[count][6], in place, with the step counts on the device:
+ * state[count][16] = m(6), v(6), step(1), 3 unused. The operation sequence is that of
+ * torch's default multi-tensor Adam for float32 CUDA tensors, with the float64
+ * hyper-parameters rounded per use as torch does, so the steps match torch's. Mirrors
+ * the optimiser the reference builds in training_setup_fix_position
+ * (scene/gaussian_model_cf.py:303-326). */
+int cfgs_pose_adam(int32_t count, float* xi, const float* grad, float* state, double lr,
+                   double beta1, double beta2, double eps, void* stream);
 
 #ifdef __cplusplus
 }

@@ -57,7 +57,7 @@ def test_invalid_arguments_rejected_on_host():
     assert lib.cfgs_render_forward(None, None, None, None, None, 0, None, None, None, None) == 1
     assert lib.cfgs_mark_visible(-1, None, None, None, None, None) == 1
     assert lib.cfgs_pose_grad(5, None, None, None, None, None, None, None, None) == 1
-    assert lib.cfgs_pose_adam(None, None, None, 1e-3, 0.9, 0.999, 1e-15, None) == 1
+    assert lib.cfgs_pose_adam(1, None, None, None, 1e-3, 0.9, 0.999, 1e-15, None) == 1
 
 
 def test_dropin_validates_argument_combinations():
