@@ -74,6 +74,29 @@ class Counts(C.Structure):
     _fields_ = [("num_rendered", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class BatchScene(C.Structure):
+    _fields_ = [("image_width", C.c_int32), ("image_height", C.c_int32), ("tanfovx", C.c_float),
+                ("tanfovy", C.c_float), ("viewmatrix", _fp), ("projmatrix", _fp), ("campos", _fp), ("bg", _fp),
+                ("sh_degree", C.c_int32), ("sh_coeffs", C.c_int32), ("num_gaussians", C.c_int32)]
+
+
+class BatchPlan(C.Structure):
+    _fields_ = [("num_scenes", C.c_int32), ("num_blocks", C.c_int32), ("gauss_slots", C.c_int64),
+                ("num_tiles", C.c_int32), ("pad_", C.c_int32), ("num_pixels", C.c_int64),
+                ("desc_bytes", C.c_size_t), ("pose_state_bytes", C.c_size_t), ("geom_bytes", C.c_size_t),
+                ("image_bytes", C.c_size_t)]
+
+
+class BatchArgs(C.Structure):
+    _fields_ = [("num_scenes", C.c_int32), ("num_blocks", C.c_int32), ("num_tiles", C.c_int32), ("pad_", C.c_int32),
+                ("gauss_slots", C.c_int64), ("capacity", C.c_int64), ("descs", _vp), ("block_scene", _vp),
+                ("tile_scene", _vp), ("means3D", _vp), ("opacities", _vp), ("shs", _vp), ("scales", _vp),
+                ("rotations", _vp), ("target", _vp), ("color", _vp), ("radii", _vp), ("geom", _vp), ("image", _vp),
+                ("binning", _vp), ("scratch", _vp), ("pose_partials", _vp), ("xi", _vp), ("adam_state", _vp),
+                ("pose_states", _vp), ("lr", C.c_double), ("beta1", C.c_double), ("beta2", C.c_double),
+                ("eps", C.c_double)]
+
+
 EXPORTS = {
     # name: (restype, argtypes)
     "cfgs_geom_bytes": (C.c_size_t, [C.c_int32]),
@@ -101,6 +124,10 @@ EXPORTS = {
     "cfgs_pose_scratch_bytes": (C.c_size_t, [C.c_int32]),
     "cfgs_pose_grad": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_pose_adam": (C.c_int, [C.c_int32, _vp, _vp, _vp, C.c_double, C.c_double, C.c_double, C.c_double, _vp]),
+    "cfgs_batch_plan": (C.c_int, [C.c_int32, C.POINTER(BatchScene), _vp, C.POINTER(BatchPlan), _vp, _vp, _vp, _vp,
+                                  _vp, _vp]),
+    "cfgs_batch_init": (C.c_int, [C.POINTER(BatchArgs), _vp]),
+    "cfgs_batch_iteration": (C.c_int, [C.POINTER(BatchArgs), _vp]),
 }
 
 _LIB = None

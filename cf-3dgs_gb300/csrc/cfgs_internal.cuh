@@ -136,6 +136,96 @@ struct BinningView {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Scenes. Every kernel reads its camera and image geometry through a scene
+// accessor: SingleScene (the drop-in path: one descriptor passed by value) or
+// SceneTable (batched solves: descriptors in device memory, looked up per block of
+// Gaussians and per tile). The kernels' arithmetic is the same for both.
+// Batched layout: scene s owns Gaussians [gauss_base, gauss_base + num_gaussians)
+// with gauss_base a multiple of kPreprocessBlock (blocks never straddle scenes),
+// tiles [tile_base, tile_base + num_tiles) and pixels [pix_base, pix_base + W*H);
+// per-pixel images of scene s start at pix_base (3*pix_base for colour, channel-major
+// inside the scene: [3, H, W]).
+// ---------------------------------------------------------------------------
+struct PoseState {     // per-scene rigid motion applied to the means before projection
+  double R64[9];       // rotation of exp(xi), float64 (pose-gradient terms)
+  double t64[3];
+  float R[9];          // the same, rounded to float (positions)
+  float t[3];
+};
+
+struct SceneDesc {
+  int32_t W, H, grid_x, grid_y;
+  int32_t tile_base, num_tiles;
+  int32_t gauss_base, num_gaussians;
+  int64_t pix_base;
+  int32_t sh_degree, sh_coeffs;
+  int32_t prefiltered, pad_;
+  float tanfovx, tanfovy, focal_x, focal_y, scale_modifier, inv_numel;
+  const float* V;       // [16] world_view_transform
+  const float* P;       // [16] full_proj_transform
+  const float* campos;  // [3]
+  const float* bg;      // [3]
+  const PoseState* pose;  // NULL: means3D are used as given
+};
+
+struct SingleScene {
+  SceneDesc d;
+  __device__ __forceinline__ const SceneDesc& for_block(int) const { return d; }
+  __device__ __forceinline__ const SceneDesc& for_tile(int) const { return d; }
+};
+
+struct SceneTable {
+  const SceneDesc* d;
+  const int32_t* block_scene;  // preprocess block -> scene
+  const int32_t* tile_scene;   // global tile -> scene
+  __device__ __forceinline__ const SceneDesc& for_block(int b) const { return d[block_scene[b]]; }
+  __device__ __forceinline__ const SceneDesc& for_tile(int t) const { return d[tile_scene[t]]; }
+};
+
+// Position of Gaussian i as the projection sees it: the stored mean, or R p + t in
+// the order ((R0 x + R1 y) + R2 z) + t with one rounding per operation.
+__device__ __forceinline__ float3 posed_mean(const SceneDesc& sd, const float* means, size_t i) {
+  float3 p = make_float3(means[3 * i], means[3 * i + 1], means[3 * i + 2]);
+  if (sd.pose == nullptr) return p;
+  const float* R = sd.pose->R;
+  const float* t = sd.pose->t;
+  float3 q;
+  q.x = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(R[0], p.x), __fmul_rn(R[1], p.y)), __fmul_rn(R[2], p.z)), t[0]);
+  q.y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(R[3], p.x), __fmul_rn(R[4], p.y)), __fmul_rn(R[5], p.z)), t[1]);
+  q.z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(R[6], p.x), __fmul_rn(R[7], p.y)), __fmul_rn(R[8], p.z)), t[2]);
+  return q;
+}
+
+// Host helper: the descriptor of the drop-in path's single scene.
+inline SceneDesc single_scene_desc(const CfgsSettings* s, int32_t n, int32_t sh_coeffs) {
+  SceneDesc d{};
+  d.W = s->image_width;
+  d.H = s->image_height;
+  d.grid_x = (d.W + kTileX - 1) / kTileX;
+  d.grid_y = (d.H + kTileY - 1) / kTileY;
+  d.tile_base = 0;
+  d.num_tiles = d.grid_x * d.grid_y;
+  d.gauss_base = 0;
+  d.num_gaussians = n;
+  d.pix_base = 0;
+  d.sh_degree = s->sh_degree;
+  d.sh_coeffs = sh_coeffs;
+  d.prefiltered = s->prefiltered;
+  d.tanfovx = s->tanfovx;
+  d.tanfovy = s->tanfovy;
+  d.focal_x = (float)s->image_width / (2.0f * s->tanfovx);
+  d.focal_y = (float)s->image_height / (2.0f * s->tanfovy);
+  d.scale_modifier = s->scale_modifier;
+  d.inv_numel = 1.0f / (float)(3.0 * (double)d.W * (double)d.H);
+  d.V = s->viewmatrix;
+  d.P = s->projmatrix;
+  d.campos = s->campos;
+  d.bg = s->bg;
+  d.pose = nullptr;
+  return d;
+}
+
 // Backward scratch: one 48-byte record per pre-sort instance:
 // (dxy.x, dxy.y, dconic.a, dconic.b) (dconic.c, dopacity, drgb.r, drgb.g) (drgb.b, ddepth, 0, 0)
 constexpr int kRecordFloat4 = 3;

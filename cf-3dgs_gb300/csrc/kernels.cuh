@@ -1,0 +1,114 @@
+// Kernel argument blocks and launchers shared by the drop-in entry points and the
+// batched pose-solve engine. Each launcher is defined in the translation unit that
+// holds its kernel (the forward ones are compiled without FMA contraction).
+#pragma once
+
+#include "cfgs_internal.cuh"
+
+namespace cfgs {
+
+template <class Scenes>
+struct PreArgs {
+  Scenes scenes;
+  CfgsGaussians g;  // pointers index the global (padded) Gaussian arrays
+  GeomView geom;
+  uint32_t* tile_count;
+  CfgsCounts* counts;
+  int32_t* radii;
+  int64_t total_slots;  // Gaussian slots covered by the launch (padded in batches)
+};
+
+template <class Scenes>
+struct ScatterArgs {
+  Scenes scenes;
+  int64_t total_slots;
+  GeomView geom;
+  const uint32_t* tile_range;
+  uint32_t* tile_cursor;
+  BinningView bin;
+  int64_t cap;
+  CfgsCounts* counts;
+};
+
+struct SortArgs {
+  const uint32_t* tile_range;
+  BinningView bin;
+  int64_t cap;
+  const CfgsCounts* counts;
+};
+
+template <class Scenes>
+struct RenderArgs {
+  Scenes scenes;
+  const uint32_t* tile_range;
+  const uint32_t* sorted_gid;
+  const float2* xy;
+  const float4* conic_op;
+  const float4* rgbd;
+  float* final_T;
+  uint32_t* n_contrib;
+  float* out_color;
+  float* out_depth;
+  float* out_alpha;
+  int64_t cap;
+  const CfgsCounts* counts;
+};
+
+// Render backward. The per-pixel image gradient comes either from dL_dcolor (layout
+// of out_color) or, when `target` is set, from the RGB L1 loss of the clamped render,
+// mean |clamp(color, 0, 1) - target| over the scene's 3*W*H values, formed in-kernel
+// exactly as autograd forms it: sign(clamp(c) - t) * [0 <= c <= 1] * (1 / numel).
+template <class Scenes>
+struct RenderBwdArgs {
+  Scenes scenes;
+  const uint32_t* tile_range;
+  const uint32_t* sorted_gid;
+  const uint32_t* sorted_pidx;
+  const float2* xy;
+  const float4* conic_op;
+  const float4* rgbd;
+  const float* final_T;
+  const uint32_t* n_contrib;
+  const float* dL_dcolor;
+  const float* dL_ddepth;
+  const float* dL_dalpha;
+  const float* color;   // forward output (fused L1 only)
+  const float* target;  // fused L1 target, or NULL
+  float4* records;
+  int64_t cap;
+  const CfgsCounts* counts;
+};
+
+template <class Scenes>
+struct PreBwdArgs {
+  Scenes scenes;
+  CfgsGaussians g;
+  const int32_t* radii;
+  GeomView geom;
+  const float4* records;
+  CfgsGradients out;
+  int64_t total_slots;
+  int64_t cap;
+  const CfgsCounts* counts;
+  double* pose_partials;  // pose-only form: [block][9] float64 sums; NULL for the full backward
+};
+
+template <class Scenes>
+void launch_preprocess(const PreArgs<Scenes>& a, int blocks, cudaStream_t st);
+void launch_scan(uint32_t* tile_count, uint32_t* tile_range, uint32_t* tile_cursor, int num_tiles,
+                 uint32_t* block_sums, uint32_t* block_prefix, int num_blocks, CfgsCounts* counts, cudaStream_t st);
+template <class Scenes>
+void launch_scatter(const ScatterArgs<Scenes>& a, int blocks, cudaStream_t st);
+void launch_tile_sort(const SortArgs& a, int tiles, cudaStream_t st);
+template <class Scenes>
+void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st);
+template <class Scenes>
+void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st);
+template <class Scenes>
+void launch_preprocess_bwd(const PreBwdArgs<Scenes>& a, int blocks, cudaStream_t st);
+void launch_batch_pose_init(int count, const float* xi, PoseState* states, cudaStream_t st);
+void launch_batch_pose_update(int count, const SceneDesc* descs, const double* partials, float* xi,
+                              float* adam_state, PoseState* states, const CfgsCounts* counts, int64_t cap, double lr,
+                              double b1, double b2, double eps, cudaStream_t st);
+
+}  // namespace cfgs

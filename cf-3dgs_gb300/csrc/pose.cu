@@ -143,6 +143,28 @@ __global__ void __launch_bounds__(kPoseThreads) k_pose_apply(int n, const float*
   }
 }
 
+// dL/dxi from the left-perturbation sums tot = (sum g, sum (R p) x g, w_cov):
+// d_rho = sum g, d_phi = sum (R p + t) x g + w_cov, then dL/dxi = J^T dL/dd with the
+// SE(3) left Jacobian J = [[Jl, Q], [0, Jl]] — all in float64, rounded at the end.
+__device__ void pose_grad_from_sums(const float* xi, const double* tot, float* grad_out) {
+  SE3d X;
+  double Jl[9], Q[9];
+  se3_exp(xi, &X, Jl);
+  double rho[3] = {xi[0], xi[1], xi[2]};
+  double phi[3] = {xi[3], xi[4], xi[5]};
+  se3_Q(rho, phi, Q);
+  double gr[3] = {tot[0], tot[1], tot[2]};
+  double gp[3];
+  gp[0] = tot[3] + (X.t[1] * gr[2] - X.t[2] * gr[1]) + tot[6];
+  gp[1] = tot[4] + (X.t[2] * gr[0] - X.t[0] * gr[2]) + tot[7];
+  gp[2] = tot[5] + (X.t[0] * gr[1] - X.t[1] * gr[0]) + tot[8];
+  for (int j = 0; j < 3; ++j) {
+    grad_out[j] = (float)(Jl[j] * gr[0] + Jl[3 + j] * gr[1] + Jl[6 + j] * gr[2]);
+    grad_out[3 + j] = (float)(Q[j] * gr[0] + Q[3 + j] * gr[1] + Q[6 + j] * gr[2] + Jl[j] * gp[0] +
+                              Jl[3 + j] * gp[1] + Jl[6 + j] * gp[2]);
+  }
+}
+
 struct PoseGradArgs {
   int n;
   const float* xi;
@@ -231,24 +253,7 @@ __global__ void __launch_bounds__(kPoseThreads) k_pose_grad(PoseGradArgs a) {
     const volatile double* part = a.partials;
     for (int b = 0; b < (int)gridDim.x; ++b)
       for (int k = 0; k < kPosePartials; ++k) tot[k] += part[b * kPosePartials + k];
-    SE3d X;
-    double Jl[9], Q[9];
-    se3_exp(a.xi, &X, Jl);
-    double rho[3] = {a.xi[0], a.xi[1], a.xi[2]};
-    double phi[3] = {a.xi[3], a.xi[4], a.xi[5]};
-    se3_Q(rho, phi, Q);
-    // left-perturbation gradient: d_rho = sum g; d_phi = sum (Rp + t) x g + w_cov
-    double gr[3] = {tot[0], tot[1], tot[2]};
-    double gp[3];
-    gp[0] = tot[3] + (X.t[1] * gr[2] - X.t[2] * gr[1]) + tot[6];
-    gp[1] = tot[4] + (X.t[2] * gr[0] - X.t[0] * gr[2]) + tot[7];
-    gp[2] = tot[5] + (X.t[0] * gr[1] - X.t[1] * gr[0]) + tot[8];
-    // dL/dxi = J^T dL/dd with J = [[Jl, Q], [0, Jl]]
-    for (int j = 0; j < 3; ++j) {
-      a.grad_out[j] = (float)(Jl[j] * gr[0] + Jl[3 + j] * gr[1] + Jl[6 + j] * gr[2]);
-      a.grad_out[3 + j] = (float)(Q[j] * gr[0] + Q[3 + j] * gr[1] + Q[6 + j] * gr[2] + Jl[j] * gp[0] +
-                                  Jl[3 + j] * gp[1] + Jl[6 + j] * gp[2]);
-    }
+    pose_grad_from_sums(a.xi, tot, a.grad_out);
     *a.counter = 0u;
   }
 }
@@ -260,11 +265,7 @@ __global__ void __launch_bounds__(kPoseThreads) k_pose_grad(PoseGradArgs a) {
 // with the hyper-parameters as float64 scalars rounded to float32 per use, as torch
 // passes them, so both optimisers take the same steps.
 // state per solve: m[6], v[6], step, 3 unused floats.
-__global__ void k_pose_adam(int count, float* xi, const float* grad, float* state, double lr, double b1, double b2,
-                            double eps) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= count) return;
-  float* st = state + 16 * (size_t)s;
+__device__ void adam_step6(float* xi, const float* grad, float* st, double lr, double b1, double b2, double eps) {
   const float step = st[12] + 1.0f;
   const float w1 = (float)(1.0 - b1), mul2 = (float)b2, w2 = (float)(1.0 - b2);
   const double bc1 = 1.0 - pow(b1, (double)step);
@@ -274,7 +275,7 @@ __global__ void k_pose_adam(int count, float* xi, const float* grad, float* stat
   const float eps_f = (float)eps;
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
-    const float g = grad[6 * (size_t)s + k];
+    const float g = grad[k];
     float m = st[k], v = st[6 + k];
     m = fmaf(w1, g - m, m);
     v = v * mul2;
@@ -283,9 +284,83 @@ __global__ void k_pose_adam(int count, float* xi, const float* grad, float* stat
     st[6 + k] = v;
     float denom = sqrtf(v) / bc2_sqrt;
     denom = denom + eps_f;
-    xi[6 * (size_t)s + k] = fmaf(step_size, m / denom, xi[6 * (size_t)s + k]);
+    xi[k] = fmaf(step_size, m / denom, xi[k]);
   }
   st[12] = step;
+}
+
+__global__ void k_pose_adam(int count, float* xi, const float* grad, float* state, double lr, double b1, double b2,
+                            double eps) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= count) return;
+  adam_step6(xi + 6 * (size_t)s, grad + 6 * (size_t)s, state + 16 * (size_t)s, lr, b1, b2, eps);
+}
+
+__device__ void pose_state_from_xi(const float* xi, PoseState* ps) {
+  SE3d X;
+  double Jl[9];
+  se3_exp(xi, &X, Jl);
+  for (int k = 0; k < 9; ++k) {
+    ps->R64[k] = X.R[k];
+    ps->R[k] = (float)X.R[k];
+  }
+  for (int k = 0; k < 3; ++k) {
+    ps->t64[k] = X.t[k];
+    ps->t[k] = (float)X.t[k];
+  }
+}
+
+__global__ void k_batch_pose_init(int count, const float* xi, PoseState* states) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < count) pose_state_from_xi(xi + 6 * (size_t)s, states + s);
+}
+
+// One block per solve: the solve's per-block pose partials summed in a fixed pattern
+// (thread i takes blocks i, i+256, ...; then a fixed tree), the SE(3) Jacobian
+// transpose, the Adam step and the next pose state. A solve's result depends only on
+// its own blocks, so it is the same whatever else is in the batch.
+__global__ void __launch_bounds__(256) k_batch_pose_update(const SceneDesc* descs, const double* partials,
+                                                           float* xi, float* adam_state, PoseState* states,
+                                                           const CfgsCounts* counts, int64_t cap, double lr,
+                                                           double b1, double b2, double eps) {
+  __shared__ double s_red[8][6];
+  if ((int64_t)counts->num_rendered > cap) return;  // overflowed iteration: no update
+  const int s = blockIdx.x;
+  const SceneDesc& sd = descs[s];
+  const int b0 = sd.gauss_base / kPreprocessBlock;
+  const int nb = (sd.num_gaussians + kPreprocessBlock - 1) / kPreprocessBlock;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) acc[k] += partials[(size_t)(b0 + b) * 9 + k];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_red[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot[kPosePartials];
+    for (int k = 0; k < kPosePartials; ++k) tot[k] = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+      for (int k = 0; k < 6; ++k) tot[k] += s_red[w][k];
+    float* x = xi + 6 * (size_t)s;
+    float grad[6];
+    pose_grad_from_sums(x, tot, grad);
+    adam_step6(x, grad, adam_state + 16 * (size_t)s, lr, b1, b2, eps);
+    pose_state_from_xi(x, states + s);
+  }
+}
+
+void launch_batch_pose_init(int count, const float* xi, PoseState* states, cudaStream_t st) {
+  k_batch_pose_init<<<div_up(count, 128), 128, 0, st>>>(count, xi, states);
+}
+void launch_batch_pose_update(int count, const SceneDesc* descs, const double* partials, float* xi,
+                              float* adam_state, PoseState* states, const CfgsCounts* counts, int64_t cap, double lr,
+                              double b1, double b2, double eps, cudaStream_t st) {
+  k_batch_pose_update<<<count, 256, 0, st>>>(descs, partials, xi, adam_state, states, counts, cap, lr, b1, b2, eps);
 }
 
 }  // namespace cfgs

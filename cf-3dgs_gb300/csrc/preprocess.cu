@@ -11,6 +11,7 @@
 // (covariance), utils/sh_utils.py:57-112 (SH), scene/cameras.py:57-74 and
 // utils/graphics_utils.py:85-113 (camera matrices).
 #include "cfgs_internal.cuh"
+#include "kernels.cuh"
 
 namespace cfgs {
 
@@ -168,17 +169,6 @@ __device__ __forceinline__ float3 sh_to_rgb(int deg, const float* sh, float3 p, 
   return make_float3(fmaxf(r, 0.0f), fmaxf(g, 0.0f), fmaxf(bl, 0.0f));
 }
 
-struct PreArgs {
-  CfgsSettings s;
-  CfgsGaussians g;
-  GeomView geom;
-  uint32_t* tile_count;
-  CfgsCounts* counts;
-  int32_t* radii;
-  int grid_x, grid_y;
-  float focal_x, focal_y;
-};
-
 __device__ __forceinline__ uint32_t block_reduce_sum_u32(uint32_t v, uint32_t* sh_warp) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -191,23 +181,30 @@ __device__ __forceinline__ uint32_t block_reduce_sum_u32(uint32_t v, uint32_t* s
   return t;  // valid in thread 0
 }
 
-__global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs a) {
+template <class Scenes>
+__global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs<Scenes> a) {
   __shared__ uint32_t sh_warp[kPreprocessBlock / 32];
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int N = a.g.num_gaussians;
+  const SceneDesc& sd = a.scenes.for_block(blockIdx.x);
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = idx - sd.gauss_base < sd.num_gaussians;
   uint32_t touched = 0;
-  if (idx < N) {
+  if (valid) {
     int radius = 0;
-    CamConst cam;
-    load_cam(a.s, cam);
-    const float* mp = a.g.means3D + 3 * (size_t)idx;
-    float3 p = make_float3(mp[0], mp[1], mp[2]);
-    float3 t = xform43(cam.V, p);
+    float V[16], P[16], campos[3];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) V[i] = __ldg(sd.V + i);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) P[i] = __ldg(sd.P + i);
+    campos[0] = sd.campos ? __ldg(sd.campos + 0) : 0.f;
+    campos[1] = sd.campos ? __ldg(sd.campos + 1) : 0.f;
+    campos[2] = sd.campos ? __ldg(sd.campos + 2) : 0.f;
+    float3 p = posed_mean(sd, a.g.means3D, (size_t)idx);
+    float3 t = xform43(V, p);
     bool culled = t.z <= CFGS_NEAR_Z;
-    if (culled && a.s.prefiltered) atomicOr(&a.counts->flags, CFGS_FLAG_FRUSTUM_VIOLATION);
+    if (culled && sd.prefiltered) atomicOr(&a.counts->flags, CFGS_FLAG_FRUSTUM_VIOLATION);
     if (!culled) {
-      float3 hom = xform43(cam.P, p);
-      float hw = xform_w(cam.P, p);
+      float3 hom = xform43(P, p);
+      float hw = xform_w(P, p);
       float w_inv = 1.0f / (hw + 0.0000001f);
       float3 proj = make_float3(hom.x * w_inv, hom.y * w_inv, hom.z * w_inv);
       float cov[6];
@@ -219,9 +216,9 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs a) {
         const float* s = a.g.scales + 3 * (size_t)idx;
         const float* qp = a.g.rotations + 4 * (size_t)idx;
         float4 q = make_float4(qp[0], qp[1], qp[2], qp[3]);
-        cov3d_from_scale_rot(make_float3(s[0], s[1], s[2]), a.s.scale_modifier, q, cov);
+        cov3d_from_scale_rot(make_float3(s[0], s[1], s[2]), sd.scale_modifier, q, cov);
       }
-      float3 c2 = cov2d(t, a.focal_x, a.focal_y, a.s.tanfovx, a.s.tanfovy, cov, cam.V);
+      float3 c2 = cov2d(t, sd.focal_x, sd.focal_y, sd.tanfovx, sd.tanfovy, cov, V);
       float det = c2.x * c2.z - c2.y * c2.y;
       if (det != 0.0f) {
         float det_inv = 1.0f / det;
@@ -231,12 +228,12 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs a) {
         float l1 = mid + disc, l2 = mid - disc;
         float rad_f = ceilf(3.0f * sqrtf(fmaxf(l1, l2)));
         int rad = (int)rad_f;
-        float2 pimg = make_float2(ndc2pix(proj.x, a.s.image_width), ndc2pix(proj.y, a.s.image_height));
+        float2 pimg = make_float2(ndc2pix(proj.x, sd.W), ndc2pix(proj.y, sd.H));
         float rf = (float)rad;
-        int rminx = min(a.grid_x, max(0, (int)((pimg.x - rf) / (float)kTileX)));
-        int rminy = min(a.grid_y, max(0, (int)((pimg.y - rf) / (float)kTileY)));
-        int rmaxx = min(a.grid_x, max(0, (int)(((pimg.x + rf) + (float)(kTileX - 1)) / (float)kTileX)));
-        int rmaxy = min(a.grid_y, max(0, (int)(((pimg.y + rf) + (float)(kTileY - 1)) / (float)kTileY)));
+        int rminx = min(sd.grid_x, max(0, (int)((pimg.x - rf) / (float)kTileX)));
+        int rminy = min(sd.grid_y, max(0, (int)((pimg.y - rf) / (float)kTileY)));
+        int rmaxx = min(sd.grid_x, max(0, (int)(((pimg.x + rf) + (float)(kTileX - 1)) / (float)kTileX)));
+        int rmaxy = min(sd.grid_y, max(0, (int)(((pimg.y + rf) + (float)(kTileY - 1)) / (float)kTileY)));
         uint32_t area = (uint32_t)((rmaxx - rminx) * (rmaxy - rminy));
         if (area > 0) {
           float3 rgb;
@@ -245,7 +242,7 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs a) {
             const float* c = a.g.colors_precomp + 3 * (size_t)idx;
             rgb = make_float3(c[0], c[1], c[2]);
           } else {
-            rgb = sh_to_rgb(a.s.sh_degree, a.g.shs + (size_t)idx * a.g.sh_coeffs * 3, p, cam.campos, &cl);
+            rgb = sh_to_rgb(sd.sh_degree, a.g.shs + (size_t)idx * sd.sh_coeffs * 3, p, campos, &cl);
           }
           a.geom.xy[idx] = pimg;
           a.geom.conic_op[idx] = make_float4(conic.x, conic.y, conic.z, a.g.opacities[idx]);
@@ -255,17 +252,28 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs a) {
           a.geom.clamped[idx] = cl;
           touched = area;
           radius = rad;
+          uint32_t* counts = a.tile_count + sd.tile_base;
           for (int ty = rminy; ty < rmaxy; ++ty)
-            for (int tx = rminx; tx < rmaxx; ++tx) atomicAdd(&a.tile_count[ty * a.grid_x + tx], 1u);
+            for (int tx = rminx; tx < rmaxx; ++tx) atomicAdd(&counts[ty * sd.grid_x + tx], 1u);
         }
       }
     }
     a.radii[idx] = radius;
+  }
+  if (idx < a.total_slots) {
     a.geom.touched[idx] = touched;
+    if (!valid) a.radii[idx] = 0;
   }
   uint32_t bs = block_reduce_sum_u32(touched, sh_warp);
   if (threadIdx.x == 0) a.geom.block_sums[blockIdx.x] = bs;
 }
+
+template <class Scenes>
+void launch_preprocess(const PreArgs<Scenes>& a, int blocks, cudaStream_t st) {
+  k_preprocess<Scenes><<<blocks, kPreprocessBlock, 0, st>>>(a);
+}
+template void launch_preprocess<SingleScene>(const PreArgs<SingleScene>&, int, cudaStream_t);
+template void launch_preprocess<SceneTable>(const PreArgs<SceneTable>&, int, cudaStream_t);
 
 // Exclusive scan of `n` uint32 values by one block of 1024 threads; returns the total.
 __device__ uint64_t block_exclusive_scan(const uint32_t* in, uint32_t* out, int n, uint32_t* sh) {
@@ -329,6 +337,12 @@ __global__ void __launch_bounds__(256) k_mark_visible(int n, const float* means,
   vis[i] = t.z <= CFGS_NEAR_Z ? 0 : 1;
 }
 
+void launch_scan(uint32_t* tile_count, uint32_t* tile_range, uint32_t* tile_cursor, int num_tiles,
+                 uint32_t* block_sums, uint32_t* block_prefix, int num_blocks, CfgsCounts* counts, cudaStream_t st) {
+  k_scan<<<1, 1024, 0, st>>>(tile_count, tile_range, tile_cursor, num_tiles, block_sums, block_prefix, num_blocks,
+                             counts);
+}
+
 }  // namespace cfgs
 
 using namespace cfgs;
@@ -386,18 +400,15 @@ extern "C" int cfgs_preprocess_forward(const CfgsSettings* s, const CfgsGaussian
   if (cudaMemsetAsync(iv.tile_count, 0, sizeof(uint32_t) * IL.num_tiles, st) != cudaSuccess)
     return CFGS_ERR_LAUNCH;
   if (g->num_gaussians > 0) {
-    PreArgs a;
-    a.s = *s;
+    PreArgs<SingleScene> a;
+    a.scenes.d = single_scene_desc(s, g->num_gaussians, g->sh_coeffs);
     a.g = *g;
     a.geom = gv;
     a.tile_count = iv.tile_count;
     a.counts = iv.counts;
     a.radii = radii;
-    a.grid_x = IL.grid_x;
-    a.grid_y = IL.grid_y;
-    a.focal_x = (float)s->image_width / (2.0f * s->tanfovx);
-    a.focal_y = (float)s->image_height / (2.0f * s->tanfovy);
-    k_preprocess<<<GL.num_blocks, kPreprocessBlock, 0, st>>>(a);
+    a.total_slots = g->num_gaussians;
+    k_preprocess<SingleScene><<<GL.num_blocks, kPreprocessBlock, 0, st>>>(a);
     CFGS_CHECK_LAUNCH(s->debug, st);
   }
   k_scan<<<1, 1024, 0, st>>>(iv.tile_count, iv.tile_range, iv.tile_cursor, IL.num_tiles,

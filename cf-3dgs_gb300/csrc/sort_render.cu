@@ -11,9 +11,12 @@
 // Gaussian touches a tile once, so the result is exactly the order a stable sort of
 // upstream's keys gives: depth, ties broken by Gaussian index.
 //
+// Every kernel is a template over the scene accessor (one scene for the drop-in path,
+// a descriptor table for batched solves); the arithmetic is the same for both.
 // Compiled with -fmad=false; the fmaf() calls are the only fused operations, and the
 // CPU oracle performs the same sequence.
 #include "cfgs_internal.cuh"
+#include "kernels.cuh"
 
 namespace cfgs {
 
@@ -40,42 +43,79 @@ __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* sh
   return pre + (x - v);
 }
 
-struct ScatterArgs {
-  int32_t n;
-  GeomView geom;
-  const uint32_t* tile_range;
-  uint32_t* tile_cursor;
-  int grid_x;
-  BinningView bin;
-  int64_t cap;
-  CfgsCounts* counts;
-};
-
-// One thread per Gaussian (same 256-wide partition as the preprocess, so the block
-// prefixes line up): assigns pre-sort instance indices in Gaussian order, row-major
-// over the tile rectangle, and drops each instance into its tile's range.
-__global__ void __launch_bounds__(kPreprocessBlock) k_scatter(ScatterArgs a) {
+// One thread per Gaussian slot (the preprocess's 256-wide partition, so the block
+// prefixes line up) assigns pre-sort instance indices in Gaussian order, row-major over
+// the tile rectangle. The instances are then emitted warp-cooperatively: the warp's
+// instances are dealt out 32 per round, one per lane, so every round issues 32
+// independent slot reservations; lanes that hit the same tile in a round share one
+// atomicAdd (match_any). Positions inside a tile's range are arbitrary here — the tile
+// sort imposes the order.
+template <class Scenes>
+__global__ void __launch_bounds__(kPreprocessBlock) k_scatter(ScatterArgs<Scenes> a) {
   __shared__ uint32_t sh[kPreprocessBlock / 32];
+  __shared__ uint32_t s_start[kPreprocessBlock];
+  __shared__ uint32_t s_off[kPreprocessBlock];
+  __shared__ uint2 s_rect[kPreprocessBlock];
+  __shared__ uint32_t s_dbits[kPreprocessBlock];
   if ((int64_t)a.counts->num_rendered > a.cap) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.counts->flags, CFGS_FLAG_CAPACITY_OVERFLOW);
     return;
   }
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t t = g < a.n ? a.geom.touched[g] : 0u;
+  const SceneDesc& sd = a.scenes.for_block(blockIdx.x);
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
+  uint32_t t = g < a.total_slots ? a.geom.touched[g] : 0u;
   uint32_t tot;
   uint32_t off = a.geom.block_prefix[blockIdx.x] + block_excl_scan_256(t, sh, &tot);
-  if (g < a.n) a.geom.offset[g] = off;
-  if (t == 0) return;
-  uint2 r = a.geom.rect[g];
-  int x0 = r.x & 0xffff, y0 = r.x >> 16, x1 = r.y & 0xffff, y1 = r.y >> 16;
-  uint64_t dbits = (uint64_t)__float_as_uint(a.geom.rgbd[g].w) << 32;
-  uint32_t j = off;
-  for (int ty = y0; ty < y1; ++ty) {
-    for (int tx = x0; tx < x1; ++tx, ++j) {
-      int tile = ty * a.grid_x + tx;
-      uint32_t pos = a.tile_range[tile] + atomicAdd(&a.tile_cursor[tile], 1u);
-      a.bin.keys[pos] = dbits | j;
-      a.bin.inst_gid[j] = (uint32_t)g;
+  if (g < a.total_slots) a.geom.offset[g] = off;
+  // warp-inclusive scan of t -> each lane's first warp-local instance
+  uint32_t x = t;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  const uint32_t warp_total = __shfl_sync(0xffffffffu, x, 31);
+  s_start[threadIdx.x] = x - t;
+  s_off[threadIdx.x] = off;
+  s_rect[threadIdx.x] = t ? a.geom.rect[g] : make_uint2(0u, 0u);
+  s_dbits[threadIdx.x] = t ? __float_as_uint(a.geom.rgbd[g].w) : 0u;
+  __syncwarp();
+  uint32_t* cursor = a.tile_cursor;
+  const uint32_t* range = a.tile_range;
+  for (uint32_t base = 0; base < warp_total; base += 32) {
+    const uint32_t w = base + lane;
+    const bool active = w < warp_total;
+    uint32_t tile = 0xffffffffu, pidx = 0, gid = 0, dbits = 0;
+    if (active) {
+      // owner lane: the last lane whose start <= w (lanes with t == 0 share starts)
+      int lo = 0, hi = 31;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (s_start[wbase + mid] <= w) lo = mid;
+        else hi = mid - 1;
+      }
+      const int ol = wbase + lo;
+      const uint32_t j = w - s_start[ol];
+      const uint2 r = s_rect[ol];
+      const uint32_t x0 = r.x & 0xffffu, y0 = r.x >> 16, x1 = r.y & 0xffffu;
+      const uint32_t rw = x1 - x0;
+      const uint32_t ty = y0 + j / rw, tx = x0 + j % rw;
+      tile = (uint32_t)sd.tile_base + ty * (uint32_t)sd.grid_x + tx;
+      pidx = s_off[ol] + j;
+      gid = (uint32_t)((int64_t)blockIdx.x * blockDim.x + ol);
+      dbits = s_dbits[ol];
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (active) {
+      const unsigned peers = __match_any_sync(act, tile);
+      const int leader = __ffs(peers) - 1;
+      const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+      uint32_t slot = 0;
+      if (lane == leader) slot = atomicAdd(&cursor[tile], (uint32_t)__popc(peers));
+      slot = __shfl_sync(peers, slot, leader) + rank;
+      const uint32_t pos = range[tile] + slot;
+      a.bin.keys[pos] = ((uint64_t)dbits << 32) | pidx;
+      a.bin.inst_gid[pidx] = gid;
     }
   }
 }
@@ -116,16 +156,10 @@ __device__ __forceinline__ int merge_split(const uint64_t* A, int la, const uint
   return lo;
 }
 
-struct SortArgs {
-  const uint32_t* tile_range;
-  BinningView bin;
-  int64_t cap;
-  const CfgsCounts* counts;
-};
-
-// One block per tile. Segments of at most kSortCap instances: bitonic sort in shared
-// memory. Larger segments: bitonic-sort kSortCap chunks, then merge them pairwise
-// (merge path, ping-pong between keys and keys_alt) inside the block.
+// One block per tile (global tile index: scene-agnostic). Segments of at most kSortCap
+// instances: bitonic sort in shared memory. Larger segments: bitonic-sort kSortCap
+// chunks, then merge them pairwise (merge path, ping-pong between keys and keys_alt)
+// inside the block.
 __global__ void __launch_bounds__(kSortThreads) k_tile_sort(SortArgs a) {
   __shared__ uint64_t s[kSortCap];
   if ((int64_t)a.counts->num_rendered > a.cap) return;
@@ -188,36 +222,22 @@ __global__ void __launch_bounds__(kSortThreads) k_tile_sort(SortArgs a) {
   }
 }
 
-struct RenderArgs {
-  int W, H, grid_x;
-  const float* bg;
-  const uint32_t* tile_range;
-  const uint32_t* sorted_gid;
-  const float2* xy;
-  const float4* conic_op;
-  const float4* rgbd;
-  float* final_T;
-  uint32_t* n_contrib;
-  float* out_color;
-  float* out_depth;
-  float* out_alpha;
-  int64_t cap;
-  const CfgsCounts* counts;
-};
-
 // One block per 16x16 tile, one thread per pixel. Batches of 256 instances are
 // gathered into shared memory (per-Gaussian data stays L2-resident); compositing runs
 // front to back with the published thresholds; the block leaves as soon as every
 // pixel is saturated (block-wide vote).
-__global__ void __launch_bounds__(kTilePixels) k_render_fwd(RenderArgs a) {
+template <class Scenes>
+__global__ void __launch_bounds__(kTilePixels) k_render_fwd(RenderArgs<Scenes> a) {
   __shared__ float2 s_xy[kRenderBatch];
   __shared__ float4 s_co[kRenderBatch];
   __shared__ float4 s_rgbd[kRenderBatch];
   if ((int64_t)a.counts->num_rendered > a.cap) return;
   const int tile = blockIdx.x;
-  const int px = (tile % a.grid_x) * kTileX + (threadIdx.x % kTileX);
-  const int py = (tile / a.grid_x) * kTileY + (threadIdx.x / kTileX);
-  const bool inside = px < a.W && py < a.H;
+  const SceneDesc& sd = a.scenes.for_tile(tile);
+  const int lt = tile - sd.tile_base;
+  const int px = (lt % sd.grid_x) * kTileX + (threadIdx.x % kTileX);
+  const int py = (lt / sd.grid_x) * kTileY + (threadIdx.x / kTileX);
+  const bool inside = px < sd.W && py < sd.H;
   const float pxf = (float)px, pyf = (float)py;
   const uint32_t lo = a.tile_range[tile];
   const int n = (int)(a.tile_range[tile + 1] - lo);
@@ -260,17 +280,36 @@ __global__ void __launch_bounds__(kTilePixels) k_render_fwd(RenderArgs a) {
     }
   }
   if (inside) {
-    const size_t HW = (size_t)a.W * a.H;
-    const size_t pix = (size_t)py * a.W + px;
-    a.final_T[pix] = T;
-    a.n_contrib[pix] = last;
-    a.out_color[pix] = fmaf(T, __ldg(a.bg + 0), C0);
-    a.out_color[HW + pix] = fmaf(T, __ldg(a.bg + 1), C1);
-    a.out_color[2 * HW + pix] = fmaf(T, __ldg(a.bg + 2), C2);
-    if (a.out_depth) a.out_depth[pix] = D;
-    if (a.out_alpha) a.out_alpha[pix] = 1.0f - T;
+    const size_t HW = (size_t)sd.W * sd.H;
+    const size_t pix = (size_t)py * sd.W + px;
+    const size_t gp = (size_t)sd.pix_base + pix;
+    a.final_T[gp] = T;
+    a.n_contrib[gp] = last;
+    float* col = a.out_color + 3 * (size_t)sd.pix_base;
+    col[pix] = fmaf(T, __ldg(sd.bg + 0), C0);
+    col[HW + pix] = fmaf(T, __ldg(sd.bg + 1), C1);
+    col[2 * HW + pix] = fmaf(T, __ldg(sd.bg + 2), C2);
+    if (a.out_depth) a.out_depth[gp] = D;
+    if (a.out_alpha) a.out_alpha[gp] = 1.0f - T;
   }
 }
+
+// ---- launchers (shared by the drop-in entry points and the batched engine) --------
+template <class Scenes>
+void launch_scatter(const ScatterArgs<Scenes>& a, int blocks, cudaStream_t st) {
+  k_scatter<Scenes><<<blocks, kPreprocessBlock, 0, st>>>(a);
+}
+void launch_tile_sort(const SortArgs& a, int tiles, cudaStream_t st) {
+  k_tile_sort<<<tiles, kSortThreads, 0, st>>>(a);
+}
+template <class Scenes>
+void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st) {
+  k_render_fwd<Scenes><<<tiles, kTilePixels, 0, st>>>(a);
+}
+template void launch_scatter<SingleScene>(const ScatterArgs<SingleScene>&, int, cudaStream_t);
+template void launch_scatter<SceneTable>(const ScatterArgs<SceneTable>&, int, cudaStream_t);
+template void launch_render_fwd<SingleScene>(const RenderArgs<SingleScene>&, int, cudaStream_t);
+template void launch_render_fwd<SceneTable>(const RenderArgs<SceneTable>&, int, cudaStream_t);
 
 }  // namespace cfgs
 
@@ -288,12 +327,20 @@ extern "C" int cfgs_bin_forward(const CfgsSettings* s, const CfgsGaussians* g, v
   GeomLayout GL(g->num_gaussians);
   BinningView bv(binning, capacity);
   if (g->num_gaussians > 0) {
-    ScatterArgs sa{g->num_gaussians, gv, iv.tile_range, iv.tile_cursor, IL.grid_x, bv, capacity, iv.counts};
-    k_scatter<<<GL.num_blocks, kPreprocessBlock, 0, st>>>(sa);
+    ScatterArgs<SingleScene> sa;
+    sa.scenes.d = single_scene_desc(s, g->num_gaussians, g->sh_coeffs);
+    sa.total_slots = g->num_gaussians;
+    sa.geom = gv;
+    sa.tile_range = iv.tile_range;
+    sa.tile_cursor = iv.tile_cursor;
+    sa.bin = bv;
+    sa.cap = capacity;
+    sa.counts = iv.counts;
+    launch_scatter(sa, GL.num_blocks, st);
     CFGS_CHECK_LAUNCH(s->debug, st);
   }
   SortArgs so{iv.tile_range, bv, capacity, iv.counts};
-  k_tile_sort<<<IL.num_tiles, kSortThreads, 0, st>>>(so);
+  launch_tile_sort(so, IL.num_tiles, st);
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;
 }
@@ -310,11 +357,8 @@ extern "C" int cfgs_composite_forward(const CfgsSettings* s, int32_t num_gaussia
   ImageView iv(const_cast<void*>(image), s->image_width, s->image_height);
   GeomView gv(const_cast<void*>(geom), num_gaussians);
   BinningView bv(const_cast<void*>(binning), capacity);
-  RenderArgs ra;
-  ra.W = s->image_width;
-  ra.H = s->image_height;
-  ra.grid_x = IL.grid_x;
-  ra.bg = s->bg;
+  RenderArgs<SingleScene> ra;
+  ra.scenes.d = single_scene_desc(s, num_gaussians, 0);
   ra.tile_range = iv.tile_range;
   ra.sorted_gid = bv.sorted_gid;
   ra.xy = gv.xy;
@@ -327,7 +371,7 @@ extern "C" int cfgs_composite_forward(const CfgsSettings* s, int32_t num_gaussia
   ra.out_alpha = out_alpha;
   ra.cap = capacity;
   ra.counts = iv.counts;
-  k_render_fwd<<<IL.num_tiles, kTilePixels, 0, st>>>(ra);
+  launch_render_fwd(ra, IL.num_tiles, st);
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;
 }

@@ -242,6 +242,84 @@ int cfgs_pose_grad(int32_t num_points, const float* xi, const float* xyz,
 int cfgs_pose_adam(int32_t count, float* xi, const float* grad, float* state, double lr,
                    double beta1, double beta2, double eps, void* stream);
 
+/* ---- batched pose solves ----------------------------------------------------------
+ * Many CF-3DGS pose solves (trainer/cf3dgs_trainer.py:261-285), each with its own
+ * Gaussians, camera and resolution, advance together: one call runs one Adam iteration
+ * of every solve with one launch per stage (preprocess, scan, scatter, tile sort,
+ * composite, render backward with the RGB L1 image gradient formed in-kernel, pose-only
+ * preprocess backward, per-solve pose update). Nothing synchronises, so a sequence of
+ * iterations can be captured in a CUDA graph. Per solve the arithmetic is that of the
+ * single-solve path (cfgs_pose_apply -> rasteriser -> cfgs_pose_grad -> cfgs_pose_adam).
+ *
+ * Layout: solve s owns Gaussian slots [gauss_base, gauss_base + N_s) with gauss_base a
+ * multiple of 256 (slots up to the next multiple are padding), tiles
+ * [tile_base, tile_base + T_s) and pixels [pix_base, pix_base + W_s H_s); per-pixel
+ * images of s start at pix_base (colour and target at 3 * pix_base, [3, H_s, W_s]). */
+typedef struct CfgsBatchScene {   /* host description of one solve */
+  int32_t image_width, image_height;
+  float tanfovx, tanfovy;
+  const float* viewmatrix;  /* device [16] */
+  const float* projmatrix;  /* device [16] */
+  const float* campos;      /* device [3]  */
+  const float* bg;          /* device [3]  */
+  int32_t sh_degree, sh_coeffs;
+  int32_t num_gaussians;
+} CfgsBatchScene;
+
+typedef struct CfgsBatchPlan {    /* sizes of a batch, filled by cfgs_batch_plan */
+  int32_t num_scenes;
+  int32_t num_blocks;        /* 256-wide Gaussian blocks = gauss_slots / 256     */
+  int64_t gauss_slots;
+  int32_t num_tiles;
+  int32_t pad_;
+  int64_t num_pixels;
+  size_t desc_bytes;         /* scene table (device copy of the host table)      */
+  size_t pose_state_bytes;   /* per-solve pose state                             */
+  size_t geom_bytes, image_bytes;
+} CfgsBatchPlan;
+
+/* Host-only: computes the plan and, when the output pointers are non-null, the host
+ * images of the scene table (desc_host, plan.desc_bytes), the block->solve map
+ * (block_scene_host, num_blocks int32) and the tile->solve map (tile_scene_host,
+ * num_tiles int32), plus per-solve bases (gauss_base, tile_base: int32 [S];
+ * pix_base: int64 [S]). `pose_states_device` is where the caller will keep the pose
+ * states (plan.pose_state_bytes) on the device. */
+int cfgs_batch_plan(int32_t num_scenes, const CfgsBatchScene* scenes, const void* pose_states_device,
+                    CfgsBatchPlan* plan, void* desc_host, int32_t* block_scene_host, int32_t* tile_scene_host,
+                    int32_t* gauss_base, int32_t* tile_base, int64_t* pix_base);
+
+typedef struct CfgsBatchArgs {    /* device pointers of one batch */
+  int32_t num_scenes, num_blocks, num_tiles, pad_;
+  int64_t gauss_slots, capacity;
+  const void* descs;              /* scene table, plan.desc_bytes               */
+  const int32_t* block_scene;
+  const int32_t* tile_scene;
+  const float* means3D;           /* [slots,3] un-posed positions              */
+  const float* opacities;         /* [slots]                                   */
+  const float* shs;               /* [slots,M,3] (M = the solves' sh_coeffs)   */
+  const float* scales;            /* [slots,3]                                 */
+  const float* rotations;         /* [slots,4]                                 */
+  const float* target;            /* [3 * num_pixels]                          */
+  float* color;                   /* [3 * num_pixels] render of the iteration  */
+  int32_t* radii;                 /* [slots]                                   */
+  void* geom;                     /* plan.geom_bytes                           */
+  void* image;                    /* plan.image_bytes                          */
+  void* binning;                  /* cfgs_binning_bytes(capacity)              */
+  void* scratch;                  /* cfgs_backward_scratch_bytes(capacity)     */
+  double* pose_partials;          /* [num_blocks][9]                           */
+  float* xi;                      /* [S][6] tangents, updated in place         */
+  float* adam_state;              /* [S][16] (cfgs_pose_adam layout)           */
+  void* pose_states;              /* plan.pose_state_bytes                     */
+  double lr, beta1, beta2, eps;
+} CfgsBatchArgs;
+
+/* Sets every solve's pose state from xi (call once before the first iteration). */
+int cfgs_batch_init(const CfgsBatchArgs* args, void* stream);
+/* One Adam iteration of every solve. K (all solves' tile instances together) above
+ * `capacity` raises CFGS_FLAG_CAPACITY_OVERFLOW in the image workspace's counts (read
+ * with cfgs_read_counts); that iteration's update is then skipped. */
+int cfgs_batch_iteration(const CfgsBatchArgs* args, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
