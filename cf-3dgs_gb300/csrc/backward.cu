@@ -61,21 +61,27 @@ __device__ __forceinline__ float l1_grad(float c, float t, float inv_numel) {
   return (c >= 0.0f && c <= 1.0f) ? inv_numel * sgn : 0.0f;
 }
 
+// Same pixel boxes and exact shortcuts as the forward (box_may_contribute per warp and
+// instance, alpha_threshold per pixel); the cross-warp sum of an instance adds only the
+// warps that kept it (the others' terms are exact zeros).
 template <class Scenes>
 __global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes> a) {
-  __shared__ float2 s_xy[kBwdBatch];
+  __shared__ float4 s_xyt[kBwdBatch];
   __shared__ float4 s_co[kBwdBatch];
   __shared__ float4 s_rgbd[kBwdBatch];
   __shared__ uint32_t s_pidx[kBwdBatch];
   __shared__ float s_part[kWarps][kBwdBatch][10];
+  __shared__ uint32_t s_keep[kWarps][kBwdBatch / 32];
   __shared__ uint32_t s_max;
   if ((int64_t)a.counts->num_rendered > a.cap) return;
   const int tile = blockIdx.x;
   const SceneDesc& sd = a.scenes.for_tile(tile);
   const int lt = tile - sd.tile_base;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int px = (lt % sd.grid_x) * kTileX + (threadIdx.x % kTileX);
-  const int py = (lt / sd.grid_x) * kTileY + (threadIdx.x / kTileX);
+  const int bx0 = (lt % sd.grid_x) * kTileX + (warp & 1) * 8;
+  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 4;
+  const int px = bx0 + (lane & 7), py = by0 + (lane >> 3);
+  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 3);
   const bool inside = px < sd.W && py < sd.H;
   const float pxf = (float)px, pyf = (float)py;
   const uint32_t lo = a.tile_range[tile];
@@ -122,25 +128,45 @@ __global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes
       uint32_t i = lo + base + threadIdx.x;
       uint32_t g = a.sorted_gid[i];
       s_pidx[threadIdx.x] = a.sorted_pidx[i];
-      s_xy[threadIdx.x] = a.xy[g];
+      float2 m = a.xy[g];
       float4 co = a.conic_op[g];
+      s_xyt[threadIdx.x] = make_float4(m.x, m.y, alpha_threshold(co.w), 0.0f);
       s_co[threadIdx.x] = make_float4(-0.5f * co.x, -co.y, -0.5f * co.z, co.w);
       s_rgbd[threadIdx.x] = a.rgbd[g];
     }
     __syncthreads();
-    for (int j = cnt - 1; j >= 0; --j) {
+    uint32_t keep[kBwdBatch / 32];
+#pragma unroll
+    for (int r = 0; r < kBwdBatch / 32; ++r) {
+      const int j = r * 32 + lane;
+      bool k = false;
+      if (j < cnt) {
+        const float4 xyt = s_xyt[j];
+        const float4 co = s_co[j];
+        k = box_may_contribute(make_float2(xyt.x, xyt.y), co.x, co.y, co.z, xyt.z, bxf0, bxf1, byf0, byf1);
+      }
+      keep[r] = __ballot_sync(0xffffffffu, k);
+      if (lane == 0) s_keep[warp][r] = keep[r];
+    }
+#pragma unroll
+    for (int r = kBwdBatch / 32 - 1; r >= 0; --r) {
+     uint32_t mk = keep[r];
+     while (mk) {
+      const int bit = 31 - __clz(mk);
+      mk &= ~(1u << bit);
+      const int j = r * 32 + bit;
       const int c = base + j;
       float v[16];
 #pragma unroll
       for (int k = 0; k < 16; ++k) v[k] = 0.f;
       bool contrib = false;
       if (c < (int)last) {
-        float2 m = s_xy[j];
+        const float4 m = s_xyt[j];
         float4 co = s_co[j];
         float dx = m.x - pxf, dy = m.y - pyf;
         float power = gauss_power(co.x, co.y, co.z, dx, dy);
-        if (power <= 0.0f) {
-          float G = exp_ref(power);
+        if (!(power > 0.0f || power < m.z)) {
+          float G = exp_ref_inrange(power);
           float alpha = fminf(CFGS_ALPHA_MAX, co.w * G);
           if (alpha >= CFGS_ALPHA_MIN) {
             contrib = true;
@@ -184,16 +210,19 @@ __global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes
       } else if (lane < 10) {
         s_part[warp][j][lane] = 0.f;
       }
+     }
     }
     __syncthreads();
     if ((int)threadIdx.x < cnt) {
+      const int j = threadIdx.x;
       float sum[10];
 #pragma unroll
       for (int k = 0; k < 10; ++k) sum[k] = 0.f;
 #pragma unroll
       for (int w = 0; w < kWarps; ++w)
+        if ((s_keep[w][j >> 5] >> (j & 31)) & 1u)
 #pragma unroll
-        for (int k = 0; k < 10; ++k) sum[k] += s_part[w][threadIdx.x][k];
+          for (int k = 0; k < 10; ++k) sum[k] += s_part[w][j][k];
       float4* rec = a.records + (size_t)kRecordFloat4 * s_pidx[threadIdx.x];
       rec[0] = make_float4(sum[0], sum[1], sum[2], sum[3]);
       rec[1] = make_float4(sum[4], sum[5], sum[6], sum[7]);

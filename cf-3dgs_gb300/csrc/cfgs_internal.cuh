@@ -275,6 +275,62 @@ __device__ __forceinline__ float gauss_power(float ca, float cb, float cc, float
   return fmaf(ca * dx, dx, e);
 }
 
+// exp_ref for x in [-103, 0] (and NaN): the same operation sequence without the range
+// guards, and the scaling by 2^k as one multiply — exact, and equal to exp_ref's
+// two-step scaling, whenever the result is a normal float (k >= -125), which holds
+// for every x the render kernels pass (see alpha_threshold).
+__device__ __forceinline__ float exp_ref_inrange(float x) {
+  const float kLog2e = 1.4426950216293335f;
+  const float kLn2Hi = 0.693145751953125f;
+  const float kLn2Lo = 1.428606765330187e-06f;
+  float kf = rintf(x * kLog2e);
+  float r = fmaf(-kf, kLn2Hi, x);
+  r = fmaf(-kf, kLn2Lo, r);
+  float p = 0.00019841270113829523f;
+  p = fmaf(p, r, 0.0013888889225199819f);
+  p = fmaf(p, r, 0.008333333767950535f);
+  p = fmaf(p, r, 0.0416666679084301f);
+  p = fmaf(p, r, 0.1666666716337204f);
+  p = fmaf(p, r, 0.5f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  return p * __int_as_float(((int)kf + 127) << 23);
+}
+
+// Lower bound on the exponent of a Gaussian of opacity o that can still give
+// alpha >= 1/255: below it, min(0.99, o exp_ref(power)) < 1/255 for certain, so the
+// pixel can skip the exponential without changing any output. The bound sits 1e-3
+// (in log space) under ln(1/(255 o)), far outside float error, and is clamped to
+// -74 so the exponentials that do run stay in exp_ref_inrange's exact range; the
+// clamp never hides a contribution for o <= 1e29.
+__device__ __forceinline__ float alpha_threshold(float o) {
+  float t = -logf(255.0f * o) - 1e-3f;
+  return t != t ? -74.0f : fmaxf(t, -74.0f);
+}
+
+// Can any pixel of the box [x0, x1] x [y0, y1] get alpha >= 1/255 from the Gaussian
+// centred at m with exponent power(d) = ca dx^2 + cb dx dy + cc dy^2 (d = m - pixel)?
+// Maximises the concave exponent over the box (the centre if inside, otherwise the best
+// point of each edge) and compares with the threshold tau with a 0.05 margin. Returns
+// true (keep) whenever the quadratic is not negative definite.
+__device__ __forceinline__ bool box_may_contribute(float2 m, float ca, float cb, float cc, float tau, float x0,
+                                                   float x1, float y0, float y1) {
+  if (!(ca < 0.0f && cc < 0.0f && 4.0f * ca * cc - cb * cb > 0.0f)) return true;
+  const float dx0 = m.x - x1, dx1 = m.x - x0, dy0 = m.y - y1, dy1 = m.y - y0;
+  if (dx0 <= 0.0f && dx1 >= 0.0f && dy0 <= 0.0f && dy1 >= 0.0f) return true;
+  float best = -INFINITY;
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const float X = e ? dx1 : dx0;  // edge dx = X: maximise over dy
+    const float dy = fminf(fmaxf(-cb * X / (2.0f * cc), dy0), dy1);
+    best = fmaxf(best, ca * X * X + cb * X * dy + cc * dy * dy);
+    const float Y = e ? dy1 : dy0;  // edge dy = Y: maximise over dx
+    const float dx = fminf(fmaxf(-cb * Y / (2.0f * ca), dx0), dx1);
+    best = fmaxf(best, ca * dx * dx + cb * dx * Y + cc * Y * Y);
+  }
+  return best >= tau - 0.05f;
+}
+
 // Real spherical-harmonics constants of utils/sh_utils.py:16-40 (degrees 0..3).
 #define CFGS_SH_C0 0.28209479177387814f
 #define CFGS_SH_C1 0.4886025119029199f

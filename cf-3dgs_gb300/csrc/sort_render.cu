@@ -222,61 +222,90 @@ __global__ void __launch_bounds__(kSortThreads) k_tile_sort(SortArgs a) {
   }
 }
 
-// One block per 16x16 tile, one thread per pixel. Batches of 256 instances are
-// gathered into shared memory (per-Gaussian data stays L2-resident); compositing runs
-// front to back with the published thresholds; the block leaves as soon as every
-// pixel is saturated (block-wide vote).
+// One block per 16x16 tile, one thread per pixel; warp w covers the 8x4 pixel box
+// (8 (w & 1), 4 (w >> 1)) of the tile. Batches of 256 instances are gathered into shared
+// memory (per-Gaussian data stays L2-resident). Two exact shortcuts skip work whose
+// outcome is known: each warp keeps only the instances whose alpha >= 1/255 ellipse can
+// reach its box (box_may_contribute, one test per instance and warp), and a pixel skips
+// the exponential when the exponent lies below the instance's alpha_threshold. Neither
+// changes a decision of the published algorithm, so every output — contributor counts
+// included, which count positions in the tile's list — is what the plain loop gives.
+// Compositing runs front to back; a warp stops when its pixels are saturated and the
+// block when all are.
 template <class Scenes>
 __global__ void __launch_bounds__(kTilePixels) k_render_fwd(RenderArgs<Scenes> a) {
-  __shared__ float2 s_xy[kRenderBatch];
-  __shared__ float4 s_co[kRenderBatch];
+  __shared__ float4 s_xyt[kRenderBatch];   // (x, y, alpha threshold, -)
+  __shared__ float4 s_co[kRenderBatch];    // (ca, cb, cc, opacity)
   __shared__ float4 s_rgbd[kRenderBatch];
   if ((int64_t)a.counts->num_rendered > a.cap) return;
   const int tile = blockIdx.x;
   const SceneDesc& sd = a.scenes.for_tile(tile);
   const int lt = tile - sd.tile_base;
-  const int px = (lt % sd.grid_x) * kTileX + (threadIdx.x % kTileX);
-  const int py = (lt / sd.grid_x) * kTileY + (threadIdx.x / kTileX);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bx0 = (lt % sd.grid_x) * kTileX + (warp & 1) * 8;
+  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 4;
+  const int px = bx0 + (lane & 7), py = by0 + (lane >> 3);
+  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 3);
   const bool inside = px < sd.W && py < sd.H;
   const float pxf = (float)px, pyf = (float)py;
   const uint32_t lo = a.tile_range[tile];
   const int n = (int)(a.tile_range[tile + 1] - lo);
   bool done = !inside;
   float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f;
-  uint32_t contributor = 0, last = 0;
+  uint32_t last = 0;
   for (int base = 0; base < n; base += kRenderBatch) {
     if (__syncthreads_count(done) == kRenderBatch) break;
     int i = base + threadIdx.x;
     if (i < n) {
       uint32_t g = a.sorted_gid[lo + i];
-      s_xy[threadIdx.x] = a.xy[g];
+      float2 m = a.xy[g];
       float4 co = a.conic_op[g];
+      s_xyt[threadIdx.x] = make_float4(m.x, m.y, alpha_threshold(co.w), 0.0f);
       s_co[threadIdx.x] = make_float4(-0.5f * co.x, -co.y, -0.5f * co.z, co.w);
       s_rgbd[threadIdx.x] = a.rgbd[g];
     }
     __syncthreads();
     const int cnt = min(kRenderBatch, n - base);
-    for (int j = 0; !done && j < cnt; ++j) {
-      ++contributor;
-      float2 m = s_xy[j];
-      float4 co = s_co[j];
-      float power = gauss_power(co.x, co.y, co.z, m.x - pxf, m.y - pyf);
-      if (power > 0.0f) continue;
-      float alpha = fminf(CFGS_ALPHA_MAX, co.w * exp_ref(power));
-      if (alpha < CFGS_ALPHA_MIN) continue;
-      float test_T = T * (1.0f - alpha);
-      if (test_T < CFGS_T_MIN) {
-        done = true;
-        continue;
+    uint32_t keep[kRenderBatch / 32];
+#pragma unroll
+    for (int r = 0; r < kRenderBatch / 32; ++r) {
+      const int j = r * 32 + lane;
+      bool k = false;
+      if (j < cnt) {
+        const float4 xyt = s_xyt[j];
+        const float4 co = s_co[j];
+        k = box_may_contribute(make_float2(xyt.x, xyt.y), co.x, co.y, co.z, xyt.z, bxf0, bxf1, byf0, byf1);
       }
-      float4 c = s_rgbd[j];
-      float w = alpha * T;
-      C0 = fmaf(c.x, w, C0);
-      C1 = fmaf(c.y, w, C1);
-      C2 = fmaf(c.z, w, C2);
-      D = fmaf(c.w, w, D);
-      T = test_T;
-      last = contributor;
+      keep[r] = __ballot_sync(0xffffffffu, k);
+    }
+#pragma unroll
+    for (int r = 0; r < kRenderBatch / 32; ++r) {
+      if (__all_sync(0xffffffffu, done)) break;
+      uint32_t mk = keep[r];
+      while (mk) {
+        const int j = r * 32 + __ffs(mk) - 1;
+        mk &= mk - 1;
+        if (done) continue;
+        const float4 xyt = s_xyt[j];
+        const float4 co = s_co[j];
+        const float power = gauss_power(co.x, co.y, co.z, xyt.x - pxf, xyt.y - pyf);
+        if (power > 0.0f || power < xyt.z) continue;
+        const float alpha = fminf(CFGS_ALPHA_MAX, co.w * exp_ref_inrange(power));
+        if (alpha < CFGS_ALPHA_MIN) continue;
+        const float test_T = T * (1.0f - alpha);
+        if (test_T < CFGS_T_MIN) {
+          done = true;
+          continue;
+        }
+        const float4 c = s_rgbd[j];
+        const float w = alpha * T;
+        C0 = fmaf(c.x, w, C0);
+        C1 = fmaf(c.y, w, C1);
+        C2 = fmaf(c.z, w, C2);
+        D = fmaf(c.w, w, D);
+        T = test_T;
+        last = (uint32_t)(base + j + 1);
+      }
     }
   }
   if (inside) {
