@@ -158,6 +158,48 @@ class BatchSolver:
         self.xi.zero_()
         self.adam.zero_()
 
+    def load_state(self, xi: torch.Tensor, adam: torch.Tensor):
+        """Sets every solve's tangent [S,6] and Adam state [S,16] (to resume solves)."""
+        self.xi.copy_(xi)
+        self.adam.copy_(adam)
+
+    def launch(self, iters: int) -> torch.cuda.Event:
+        """Enqueues `iters` iterations of every solve from the current state (no reset)
+        and returns an event that completes with them. The first call sizes the
+        instance capacity from the current poses (one counting iteration)."""
+        self._saved = (self.xi.clone(), self.adam.clone(), iters)
+        if getattr(self, "_cap_ready", False) is False:
+            K0 = self.probe_capacity()
+            self.load_state(self._saved[0], self._saved[1])
+            self._alloc_instances(int(K0 * self.capacity_factor) + 4096)
+            self._cap_ready = True
+        args = self._args()
+        st = torch.cuda.current_stream(self.dev).cuda_stream
+        native.check(self.lib.cfgs_batch_init(C.byref(args), st), "cfgs_batch_init")
+        done = self._run_graph(args, iters) if (self.use_graph and iters >= self.graph_chunk) else 0
+        for _ in range(iters - done):
+            native.check(self.lib.cfgs_batch_iteration(C.byref(args), st), "cfgs_batch_iteration")
+        ev = torch.cuda.Event()
+        ev.record(torch.cuda.current_stream(self.dev))
+        return ev
+
+    def finish(self) -> bool:
+        """After launch()'s event: True if the iterations ran within capacity; otherwise
+        restores the state saved by launch() and doubles the capacity (re-launch)."""
+        if not (self._counts().flags & native.FLAG_CAPACITY_OVERFLOW):
+            return True
+        self.load_state(self._saved[0], self._saved[1])
+        self._alloc_instances(self.capacity * 2)
+        return False
+
+    def run(self, iters: int) -> bool:
+        """launch() + finish(), retrying with more capacity up to three times."""
+        for _ in range(4):
+            self.launch(iters).synchronize()
+            if self.finish():
+                return True
+        return False
+
     # ---- running -------------------------------------------------------------------
     def probe_capacity(self) -> int:
         """K of the current poses (an iteration at capacity 0 only counts; the update
