@@ -44,6 +44,10 @@ def _args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
+    p.add_argument("--workload", default="fwdbwd", choices=["fwdbwd", "pose", "batch", "serve"])
+    p.add_argument("--serve-rate", type=float, default=200.0)
+    p.add_argument("--serve-seconds", type=float, default=60.0)
+    p.add_argument("--serve-slots", type=int, default=64)
     return p.parse_args()
 
 
@@ -348,10 +352,123 @@ def run_reference(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def _pose_setup(dev, count, seed=3):
+    import diff_gaussian_rasterization  # noqa: F401
+    from cfgs import pose, scenes
+    specs = scenes.batch_specs(count, seed=seed)
+    probs, cams = [], []
+    for (w, h, n, sd) in specs:
+        sc = scenes.scene_pose(width=w, height=h, n=n, seed=sd)
+        probs.append(pose.make_problem(sc, dev))
+        cams.append(sc.camera)
+    return specs, probs, cams
+
+
+def run_pose(a) -> None:
+    """One CF-3DGS relative-pose solve (640x360, one Gaussian per pixel, 300 Adam
+    iterations, lr 1e-3, RGB L1): plain path vs fused pose kernels."""
+    import numpy as np
+    import torch
+    import diff_gaussian_rasterization  # noqa: F401
+    from cfgs import pose, scenes
+    dev = torch.device("cuda", 0)
+    prob = pose.make_problem(scenes.scene_pose(width=640, height=360, seed=2), dev)
+    res = {}
+    for mode in ("plain", "fused"):
+        pose.time_solves(prob, mode, count=1)
+        sps, lat = pose.time_solves(prob, mode, count=max(2, a.steps // 5))
+        xi, _ = pose.solve(prob, mode=mode)
+        res[mode] = {"solves_per_s": round(sps, 4), "latency_s": [round(x, 4) for x in lat], "xi": xi}
+    dang, dtr = pose.pose_error(res["plain"]["xi"], res["fused"]["xi"])
+    gerr = pose.pose_error(res["fused"]["xi"], prob.xi_gt)
+    line = {"metric": "pose solves/s (640x360, 300 iterations)", "value": res["fused"]["solves_per_s"],
+            "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "CF-3DGS relative pose solve, 230400 SH0 Gaussians, 640x360, 300 Adam iters"},
+            "plain_solves_per_s": res["plain"]["solves_per_s"],
+            "speedup_vs_plain": round(res["fused"]["solves_per_s"] / res["plain"]["solves_per_s"], 3),
+            "plain_vs_fused": {"rot_deg": dang, "trans": dtr},
+            "fused_vs_ground_truth": {"rot_deg": gerr[0], "trans": gerr[1]}}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(a) -> None:
+    """64 pose solves (N log-uniform in [5e4, 5e5], resolutions 320x180/640x360/960x540)
+    batched in one launch per stage with CUDA-graph replays, vs the same solves one by one
+    on the plain path (timed on a sample of them)."""
+    import numpy as np
+    import torch
+    from cfgs import batch, pose
+    dev = torch.device("cuda", 0)
+    specs, probs, _ = _pose_setup(dev, 64)
+    bs = batch.BatchSolver(probs)
+    bs.solve(300)
+    r = bs.solve(300)
+    sample = max(2, min(8, a.steps))
+    batch.solve_sequential(probs[:1], 300, "plain")
+    xs, lat = batch.solve_sequential(probs[:sample], 300, "plain")
+    plain_sps = sample / sum(lat)
+    xf, latf = batch.solve_sequential(probs[:sample], 300, "fused")
+    agree = [pose.pose_error(xs[i], r.xi[i]) for i in range(sample)]
+    line = {"metric": "batched pose solves/s (64 uneven solves)", "value": round(64 / r.seconds, 4),
+            "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "64 CF-3DGS pose solves, N log-uniform [5e4,5e5], 3 resolutions, 300 iters",
+                       "total_gaussians": int(sum(p.xyz.shape[0] for p in probs)), "num_rendered": r.num_rendered0,
+                       "graph_chunk": bs.graph_chunk},
+            "batch_seconds": round(r.seconds, 3), "ms_per_iteration": round(1000 * r.seconds / 300, 3),
+            "plain_sequential_solves_per_s": round(plain_sps, 4), "plain_sample": sample,
+            "fused_sequential_solves_per_s": round(sample / sum(latf), 4),
+            "speedup_vs_plain": round((64 / r.seconds) / plain_sps, 3),
+            "batched_vs_fused_single_bit_identical": bool(np.array_equal(np.float32(xf), np.float32(r.xi[:sample]))),
+            "batched_vs_plain_max": {"rot_deg": max(x[0] for x in agree), "trans": max(x[1] for x in agree)}}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(a) -> None:
+    """A Poisson stream (rate a.serve_rate req/s for a.serve_seconds s; 90% pose solves of
+    the 64-solve mix, 10% renders of a device-resident 1M-Gaussian SH3 scene at
+    1920x1080) served by the continuous-batching server and by a plain FIFO loop, each
+    for the length of the stream."""
+    import torch
+    from cfgs import scenes, serve
+    dev = torch.device("cuda", 0)
+    _, probs, cams = _pose_setup(dev, 64)
+    payloads = [serve.payload_from_problem(p, c) for p, c in zip(probs, cams)]
+    del probs
+    target = serve.RenderTarget(scenes.scene_large(), dev)
+    target.render()
+    torch.cuda.synchronize()
+    out = {}
+    for name in ("continuous", "plain_fifo"):
+        stream = serve.poisson_stream(a.serve_rate, a.serve_seconds, 0.9, len(payloads), 1, seed=11)
+        if name == "continuous":
+            srv = serve.ContinuousBatchServer(payloads, [target], dev, max_slots=a.serve_slots, hbm_budget=150e9)
+        else:
+            srv = serve.PlainFifoServer(payloads, [target], dev)
+        st = srv.run(stream, wall_limit=a.serve_seconds)
+        s = st.summary(name)
+        s["arrived"] = len(stream)
+        out[name] = s
+    c, p = out["continuous"], out["plain_fifo"]
+    line = {"metric": "served requests/s (90% pose solves, 10% 1080p renders)", "value": c["throughput_req_s"],
+            "unit": "req/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"Poisson {a.serve_rate} req/s for {a.serve_seconds} s, 90% pose solves "
+                                   "(64-solve mix), 10% renders of 1M SH3 Gaussians at 1920x1080",
+                       "hbm_budget_gb": 150, "max_slots": a.serve_slots, "epoch_iterations": 25},
+            "continuous": c, "plain_fifo": p,
+            "pose_throughput_speedup_vs_plain": round(c["pose_solves_per_s"] / max(p["pose_solves_per_s"], 1e-9), 3)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "pose":
+        run_pose(a)
+    elif a.workload == "batch":
+        run_batch(a)
+    elif a.workload == "serve":
+        run_serve(a)
     else:
         run_ours(a)
 
