@@ -27,7 +27,7 @@ COMMON_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcomp
 # Translation units whose float results the CPU oracle reproduces bit for bit are
 # compiled without FMA contraction; their fused operations are explicit fmaf() calls.
 NO_CONTRACT = {"preprocess.cu", "sort_render.cu"}
-SOURCES = ["preprocess.cu", "sort_render.cu", "backward.cu", "pose.cu", "batch.cu"]
+SOURCES = ["preprocess.cu", "sort_render.cu", "render_bwd.cu", "preprocess_bwd.cu", "pose.cu", "batch.cu"]
 
 
 def _nvcc() -> str:

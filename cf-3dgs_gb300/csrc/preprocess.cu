@@ -120,7 +120,7 @@ __device__ __forceinline__ float ndc2pix(float v, int S) { return ((v + 1.0f) * 
 
 // Colour from real SH of degree <= 3 at the view direction, + 0.5, clamped at 0.
 __device__ __forceinline__ float3 sh_to_rgb(int deg, const float* sh, float3 p, const float* campos,
-                                            uint8_t* clamped) {
+                                            uint8_t* clamped, bool vec16) {
   float dx = p.x - campos[0], dy = p.y - campos[1], dz = p.z - campos[2];
   float len = sqrtf(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
   float x = dx / len, y = dy / len, z = dz / len;
@@ -153,13 +153,36 @@ __device__ __forceinline__ float3 sh_to_rgb(int deg, const float* sh, float3 p, 
       }
     }
   }
-  float r = b[0] * sh[0], g = b[0] * sh[1], bl = b[0] * sh[2];
+  float r, g, bl;
+  if (nb == kMaxShCoeffs && vec16) {
+    // 16 coefficients, 16-byte aligned: 12 float4 loads, consumed in the same
+    // (coefficient, channel) order as the scalar path below
+    const float4* s4 = reinterpret_cast<const float4*>(sh);
+    float c[3];
 #pragma unroll
-  for (int k = 1; k < kMaxShCoeffs; ++k) {
-    if (k < nb) {
-      r = fmaf(b[k], sh[3 * k + 0], r);
-      g = fmaf(b[k], sh[3 * k + 1], g);
-      bl = fmaf(b[k], sh[3 * k + 2], bl);
+    for (int q = 0; q < 12; ++q) {
+      const float4 f = s4[q];
+      const float e[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int k = (4 * q + u) / 3, ch = (4 * q + u) % 3;
+        c[ch] = k == 0 ? b[0] * e[u] : fmaf(b[k], e[u], c[ch]);
+      }
+    }
+    r = c[0];
+    g = c[1];
+    bl = c[2];
+  } else {
+    r = b[0] * sh[0];
+    g = b[0] * sh[1];
+    bl = b[0] * sh[2];
+#pragma unroll
+    for (int k = 1; k < kMaxShCoeffs; ++k) {
+      if (k < nb) {
+        r = fmaf(b[k], sh[3 * k + 0], r);
+        g = fmaf(b[k], sh[3 * k + 1], g);
+        bl = fmaf(b[k], sh[3 * k + 2], bl);
+      }
     }
   }
   r = r + 0.5f;
@@ -242,7 +265,9 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs<Scenes>
             const float* c = a.g.colors_precomp + 3 * (size_t)idx;
             rgb = make_float3(c[0], c[1], c[2]);
           } else {
-            rgb = sh_to_rgb(sd.sh_degree, a.g.shs + (size_t)idx * sd.sh_coeffs * 3, p, campos, &cl);
+            const float* shp = a.g.shs + (size_t)idx * sd.sh_coeffs * 3;
+            rgb = sh_to_rgb(sd.sh_degree, shp, p, campos, &cl,
+                            sd.sh_coeffs == kMaxShCoeffs && (((uintptr_t)shp) & 15) == 0);
           }
           a.geom.xy[idx] = pimg;
           a.geom.conic_op[idx] = make_float4(conic.x, conic.y, conic.z, a.g.opacities[idx]);

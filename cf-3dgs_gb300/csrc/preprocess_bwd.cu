@@ -1,0 +1,431 @@
+// Backward, part 2: the per-Gaussian preprocess backward (conic -> 2D covariance ->
+// 3D covariance -> scale/rotation, projection -> mean, SH -> coefficients and view
+// direction), in a full form (all eight gradient arrays, the drop-in path) and a
+// pose-only form (dL/dmean reduced straight into SE(3) gradient terms, batched solves).
+//
+// Phase 1 sums each Gaussian's per-tile records (contiguous, in pre-sort order) one
+// warp per Gaussian: coalesced 48-byte record loads, a transposing warp reduction, the
+// sums to shared memory. Phase 2 is one thread per Gaussian. Both orders are fixed, so
+// the result is deterministic.
+#include "cfgs_internal.cuh"
+#include "kernels.cuh"
+
+namespace cfgs {
+
+// Sums 16 per-lane values across the warp in 16 shuffles; lane L ends with the total
+// of value index L >> 1.
+__device__ __forceinline__ float warp_sum16(float (&v)[16], int lane) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    bool up = lane & 16;
+    float send = up ? v[k] : v[k + 8];
+    float keep = up ? v[k + 8] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    bool up = lane & 8;
+    float send = up ? v[k] : v[k + 4];
+    float keep = up ? v[k + 4] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    bool up = lane & 4;
+    float send = up ? v[k] : v[k + 2];
+    float keep = up ? v[k + 2] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  {
+    bool up = lane & 2;
+    float send = up ? v[0] : v[1];
+    float keep = up ? v[1] : v[0];
+    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+  return v[0];
+}
+
+// SH backward at unit direction (x,y,z): dL/dsh[k][c] = b_k g_c (g already masked by
+// the forward's clamp) and the gradient of sum_k (sh_k . g) b_k with respect to the
+// direction. The basis follows utils/sh_utils.py:57-112.
+__device__ __forceinline__ void sh_backward(int deg, int M, const float* sh, float g0, float g1, float g2, float x,
+                                            float y, float z, float* dsh, float& gdx, float& gdy, float& gdz) {
+  const float xx = x * x, yy = y * y, zz = z * z, xy = x * y, yz = y * z, xz = x * z;
+  float b[16];
+  b[0] = CFGS_SH_C0;
+  b[1] = -CFGS_SH_C1 * y;
+  b[2] = CFGS_SH_C1 * z;
+  b[3] = -CFGS_SH_C1 * x;
+  b[4] = CFGS_SH_C2_0 * xy;
+  b[5] = CFGS_SH_C2_1 * yz;
+  b[6] = CFGS_SH_C2_2 * (2.f * zz - xx - yy);
+  b[7] = CFGS_SH_C2_3 * xz;
+  b[8] = CFGS_SH_C2_4 * (xx - yy);
+  b[9] = CFGS_SH_C3_0 * y * (3.f * xx - yy);
+  b[10] = CFGS_SH_C3_1 * xy * z;
+  b[11] = CFGS_SH_C3_2 * y * (4.f * zz - xx - yy);
+  b[12] = CFGS_SH_C3_3 * z * (2.f * zz - 3.f * xx - 3.f * yy);
+  b[13] = CFGS_SH_C3_4 * x * (4.f * zz - xx - yy);
+  b[14] = CFGS_SH_C3_5 * z * (xx - yy);
+  b[15] = CFGS_SH_C3_6 * x * (xx - 3.f * yy);
+  const int nb = (deg + 1) * (deg + 1);
+#pragma unroll
+  for (int k = 1; k < 16; ++k)
+    if (k >= nb) b[k] = 0.f;
+#define CFGS_SK(k) (sh[3 * (k)] * g0 + sh[3 * (k) + 1] * g1 + sh[3 * (k) + 2] * g2)
+  gdx = gdy = gdz = 0.f;
+  if (deg > 0) {
+    const float s1 = CFGS_SK(1), s2 = CFGS_SK(2), s3 = CFGS_SK(3);
+    gdy -= CFGS_SH_C1 * s1;
+    gdz += CFGS_SH_C1 * s2;
+    gdx -= CFGS_SH_C1 * s3;
+  }
+  if (deg > 1) {
+    const float s4 = CFGS_SK(4), s5 = CFGS_SK(5), s6 = CFGS_SK(6), s7 = CFGS_SK(7), s8 = CFGS_SK(8);
+    gdx += CFGS_SH_C2_0 * y * s4 - 2.f * CFGS_SH_C2_2 * x * s6 + CFGS_SH_C2_3 * z * s7 + 2.f * CFGS_SH_C2_4 * x * s8;
+    gdy += CFGS_SH_C2_0 * x * s4 + CFGS_SH_C2_1 * z * s5 - 2.f * CFGS_SH_C2_2 * y * s6 - 2.f * CFGS_SH_C2_4 * y * s8;
+    gdz += CFGS_SH_C2_1 * y * s5 + 4.f * CFGS_SH_C2_2 * z * s6 + CFGS_SH_C2_3 * x * s7;
+  }
+  if (deg > 2) {
+    const float s9 = CFGS_SK(9), s10 = CFGS_SK(10), s11 = CFGS_SK(11), s12 = CFGS_SK(12), s13 = CFGS_SK(13),
+                s14 = CFGS_SK(14), s15 = CFGS_SK(15);
+    gdx += CFGS_SH_C3_0 * 6.f * xy * s9 + CFGS_SH_C3_1 * yz * s10 - 2.f * CFGS_SH_C3_2 * xy * s11 -
+           6.f * CFGS_SH_C3_3 * xz * s12 + CFGS_SH_C3_4 * (4.f * zz - 3.f * xx - yy) * s13 +
+           2.f * CFGS_SH_C3_5 * xz * s14 + CFGS_SH_C3_6 * (3.f * xx - 3.f * yy) * s15;
+    gdy += CFGS_SH_C3_0 * (3.f * xx - 3.f * yy) * s9 + CFGS_SH_C3_1 * xz * s10 +
+           CFGS_SH_C3_2 * (4.f * zz - xx - 3.f * yy) * s11 - 6.f * CFGS_SH_C3_3 * yz * s12 -
+           2.f * CFGS_SH_C3_4 * xy * s13 - 2.f * CFGS_SH_C3_5 * yz * s14 - 6.f * CFGS_SH_C3_6 * xy * s15;
+    gdz += CFGS_SH_C3_1 * xy * s10 + 8.f * CFGS_SH_C3_2 * yz * s11 + CFGS_SH_C3_3 * (6.f * zz - 3.f * xx - 3.f * yy) * s12 +
+           8.f * CFGS_SH_C3_4 * xz * s13 + CFGS_SH_C3_5 * (xx - yy) * s14;
+  }
+#undef CFGS_SK
+  if (!dsh) return;
+  const float gc[3] = {g0, g1, g2};
+  if (M == 16 && (((uintptr_t)dsh) & 15) == 0) {
+    float4* d4 = reinterpret_cast<float4*>(dsh);
+#pragma unroll
+    for (int q = 0; q < 12; ++q) {
+      float e[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) e[u] = b[(4 * q + u) / 3] * gc[(4 * q + u) % 3];
+      d4[q] = make_float4(e[0], e[1], e[2], e[3]);
+    }
+  } else {
+    for (int k = 0; k < M; ++k) {
+      const float bk = k < 16 ? b[k] : 0.f;
+      dsh[3 * k + 0] = bk * g0;
+      dsh[3 * k + 1] = bk * g1;
+      dsh[3 * k + 2] = bk * g2;
+    }
+  }
+}
+
+// Full form: all eight gradient arrays. Pose-only form (pose_partials set): only
+// dL/dmean (through projection, covariance and SH view direction) is formed and the
+// block's SE(3) gradient terms — sum g and sum (R p) x g in float64 with the scene's
+// float64 rotation and the un-posed positions p — go to pose_partials[block].
+template <class Scenes>
+__global__ void __launch_bounds__(256) k_preprocess_bwd(PreBwdArgs<Scenes> a) {
+  __shared__ float s_acc[256][11];
+  __shared__ double s_red[8][6];
+  if ((int64_t)a.counts->num_rendered > a.cap) return;  // forward overflowed: outputs untouched
+  const SceneDesc& sd = a.scenes.for_block(blockIdx.x);
+  const bool pose_only = a.pose_partials != nullptr;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t blk0 = (int64_t)blockIdx.x * blockDim.x;
+
+  // ---- phase 1: record sums, one warp per Gaussian ---------------------------------
+  for (int gi = 0; gi < 32; ++gi) {
+    const int local = warp * 32 + gi;
+    const int64_t gidx = blk0 + local;
+    uint32_t nt = 0, off = 0;
+    if (gidx < a.total_slots && gidx - sd.gauss_base < sd.num_gaussians && a.radii[gidx] > 0) {
+      nt = a.geom.touched[gidx];
+      off = a.geom.offset[gidx];
+    }
+    if (nt == 0) {
+      if (lane < 10) s_acc[local][lane] = 0.f;
+      continue;
+    }
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = 0.f;
+    for (uint32_t r = lane; r < nt; r += 32) {
+      const float4* rec = a.records + (size_t)kRecordFloat4 * (off + r);
+      const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
+      v[0] += r0.x; v[1] += r0.y; v[2] += r0.z; v[3] += r0.w;
+      v[4] += r1.x; v[5] += r1.y; v[6] += r1.z; v[7] += r1.w;
+      v[8] += r2.x; v[9] += r2.y;
+    }
+    const float s = warp_sum16(v, lane);
+    const int k = lane >> 1;
+    if (!(lane & 1) && k < 10) s_acc[local][k] = s;
+  }
+  __syncthreads();
+
+  // ---- phase 2: one thread per Gaussian ----------------------------------------------
+  const int64_t idx = blk0 + threadIdx.x;
+  if (!pose_only && idx >= a.total_slots) return;
+  const bool valid = idx < a.total_slots && idx - sd.gauss_base < sd.num_gaussians;
+  const int M = sd.sh_coeffs;
+  const uint32_t nt = (valid && a.radii[idx] > 0) ? a.geom.touched[idx] : 0u;
+  float dmean[3] = {0.f, 0.f, 0.f};
+  if (nt == 0 && !pose_only) {
+    for (int k = 0; k < 3; ++k) {
+      a.out.dL_dmeans2D[3 * idx + k] = 0.f;
+      a.out.dL_dcolors[3 * idx + k] = 0.f;
+      a.out.dL_dmeans3D[3 * idx + k] = 0.f;
+      if (a.out.dL_dscales) a.out.dL_dscales[3 * idx + k] = 0.f;
+    }
+    a.out.dL_dopacity[idx] = 0.f;
+    for (int k = 0; k < 6; ++k) a.out.dL_dcov3D[6 * idx + k] = 0.f;
+    if (a.out.dL_drotations)
+      for (int k = 0; k < 4; ++k) a.out.dL_drotations[4 * idx + k] = 0.f;
+    if (a.out.dL_dsh)
+      for (int k = 0; k < 3 * M; ++k) a.out.dL_dsh[(size_t)idx * 3 * M + k] = 0.f;
+    return;
+  }
+  if (nt > 0) {
+    float acc[10];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) acc[k] = s_acc[threadIdx.x][k];
+    const float W = (float)sd.W, H = (float)sd.H;
+    const float dndc_x = acc[0] * (0.5f * W), dndc_y = acc[1] * (0.5f * H);
+    const float dcol[3] = {acc[6], acc[7], acc[8]};
+    if (!pose_only) {
+      a.out.dL_dmeans2D[3 * idx + 0] = dndc_x;
+      a.out.dL_dmeans2D[3 * idx + 1] = dndc_y;
+      a.out.dL_dmeans2D[3 * idx + 2] = 0.f;
+      a.out.dL_dopacity[idx] = acc[5];
+      a.out.dL_dcolors[3 * idx + 0] = dcol[0];
+      a.out.dL_dcolors[3 * idx + 1] = dcol[1];
+      a.out.dL_dcolors[3 * idx + 2] = dcol[2];
+    }
+
+    float V[16], P[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) V[i] = __ldg(sd.V + i);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) P[i] = __ldg(sd.P + i);
+    const float3 pm = posed_mean(sd, a.g.means3D, (size_t)idx);
+    const float px = pm.x, py = pm.y, pz = pm.z;
+
+    // ---- recompute view-space centre and the 2D covariance pieces ----------------
+    float t[3];
+    for (int i = 0; i < 3; ++i) t[i] = V[i] * px + V[4 + i] * py + V[8 + i] * pz + V[12 + i];
+    float cov[6];
+    float sx = 0, sy = 0, sz = 0, qr = 0, qx = 0, qy = 0, qz = 0, R[9];
+    const float mod = sd.scale_modifier;
+    if (a.g.cov3D_precomp) {
+      for (int k = 0; k < 6; ++k) cov[k] = a.g.cov3D_precomp[6 * idx + k];
+    } else {
+      sx = mod * a.g.scales[3 * idx + 0];
+      sy = mod * a.g.scales[3 * idx + 1];
+      sz = mod * a.g.scales[3 * idx + 2];
+      const float4 q4 = (((uintptr_t)a.g.rotations) & 15) == 0
+                            ? reinterpret_cast<const float4*>(a.g.rotations)[idx]
+                            : make_float4(a.g.rotations[4 * idx], a.g.rotations[4 * idx + 1],
+                                          a.g.rotations[4 * idx + 2], a.g.rotations[4 * idx + 3]);
+      qr = q4.x;
+      qx = q4.y;
+      qy = q4.z;
+      qz = q4.w;
+      R[0] = 1.f - 2.f * (qy * qy + qz * qz);
+      R[1] = 2.f * (qx * qy - qr * qz);
+      R[2] = 2.f * (qx * qz + qr * qy);
+      R[3] = 2.f * (qx * qy + qr * qz);
+      R[4] = 1.f - 2.f * (qx * qx + qz * qz);
+      R[5] = 2.f * (qy * qz - qr * qx);
+      R[6] = 2.f * (qx * qz - qr * qy);
+      R[7] = 2.f * (qy * qz + qr * qx);
+      R[8] = 1.f - 2.f * (qx * qx + qy * qy);
+      const float s3[3] = {sx, sy, sz};
+      float Mm[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Mm[3 * i + j] = R[3 * i + j] * s3[j];
+      const int ii[6] = {0, 0, 0, 1, 1, 2}, jj[6] = {0, 1, 2, 1, 2, 2};
+      for (int k = 0; k < 6; ++k) {
+        const float* u = Mm + 3 * ii[k];
+        const float* w = Mm + 3 * jj[k];
+        cov[k] = u[0] * w[0] + u[1] * w[1] + u[2] * w[2];
+      }
+    }
+    const float limx = 1.3f * sd.tanfovx, limy = 1.3f * sd.tanfovy;
+    const float txtz = t[0] / t[2], tytz = t[1] / t[2];
+    const float tx = fminf(limx, fmaxf(-limx, txtz)) * t[2];
+    const float ty = fminf(limy, fmaxf(-limy, tytz)) * t[2];
+    const float xmask = (txtz < -limx || txtz > limx) ? 0.f : 1.f;
+    const float ymask = (tytz < -limy || tytz > limy) ? 0.f : 1.f;
+    const float tz = t[2], tz2 = tz * tz, tz3 = tz2 * tz;
+    const float fx = sd.focal_x, fy = sd.focal_y;
+    const float J00 = fx / tz, J02 = -(fx * tx) / tz2, J11 = fy / tz, J12 = -(fy * ty) / tz2;
+    float T0[3], T1[3];
+    for (int j = 0; j < 3; ++j) {
+      T0[j] = J00 * V[4 * j + 0] + J02 * V[4 * j + 2];
+      T1[j] = J11 * V[4 * j + 1] + J12 * V[4 * j + 2];
+    }
+    const float S[9] = {cov[0], cov[1], cov[2], cov[1], cov[3], cov[4], cov[2], cov[4], cov[5]};
+    float u[3], v[3];
+    for (int i = 0; i < 3; ++i) {
+      u[i] = S[3 * i] * T0[0] + S[3 * i + 1] * T0[1] + S[3 * i + 2] * T0[2];
+      v[i] = S[3 * i] * T1[0] + S[3 * i + 1] * T1[1] + S[3 * i + 2] * T1[2];
+    }
+    const float ca = T0[0] * u[0] + T0[1] * u[1] + T0[2] * u[2] + 0.3f;
+    const float cb = T0[0] * v[0] + T0[1] * v[1] + T0[2] * v[2];
+    const float cc = T1[0] * v[0] + T1[1] * v[1] + T1[2] * v[2] + 0.3f;
+
+    // ---- conic (A,B,C) -> 2D covariance (a,b,c) -----------------------------------
+    const float dA = acc[2], dB = acc[3], dC = acc[4];
+    const float det = ca * cc - cb * cb;
+    const float id = 1.f / det, id2 = id * id;
+    const float da = dA * (-cc * cc * id2) + dB * (cb * cc * id2) + dC * (id - ca * cc * id2);
+    const float db = dA * (2.f * cb * cc * id2) + dB * (-id - 2.f * cb * cb * id2) + dC * (2.f * ca * cb * id2);
+    const float dc = dA * (id - ca * cc * id2) + dB * (ca * cb * id2) + dC * (-ca * ca * id2);
+
+    // ---- 2D covariance -> 3D covariance and the rows of T = J W ------------------
+    float dcov[6];
+    dcov[0] = da * T0[0] * T0[0] + db * T0[0] * T1[0] + dc * T1[0] * T1[0];
+    dcov[3] = da * T0[1] * T0[1] + db * T0[1] * T1[1] + dc * T1[1] * T1[1];
+    dcov[5] = da * T0[2] * T0[2] + db * T0[2] * T1[2] + dc * T1[2] * T1[2];
+    dcov[1] = 2.f * da * T0[0] * T0[1] + db * (T0[0] * T1[1] + T0[1] * T1[0]) + 2.f * dc * T1[0] * T1[1];
+    dcov[2] = 2.f * da * T0[0] * T0[2] + db * (T0[0] * T1[2] + T0[2] * T1[0]) + 2.f * dc * T1[0] * T1[2];
+    dcov[4] = 2.f * da * T0[1] * T0[2] + db * (T0[1] * T1[2] + T0[2] * T1[1]) + 2.f * dc * T1[1] * T1[2];
+    if (!pose_only)
+      for (int k = 0; k < 6; ++k) a.out.dL_dcov3D[6 * idx + k] = dcov[k];
+    float dT0[3], dT1[3];
+    for (int i = 0; i < 3; ++i) {
+      dT0[i] = 2.f * da * u[i] + db * v[i];
+      dT1[i] = db * u[i] + 2.f * dc * v[i];
+    }
+    float dJ00 = 0, dJ02 = 0, dJ11 = 0, dJ12 = 0;
+    for (int j = 0; j < 3; ++j) {
+      dJ00 += dT0[j] * V[4 * j + 0];
+      dJ02 += dT0[j] * V[4 * j + 2];
+      dJ11 += dT1[j] * V[4 * j + 1];
+      dJ12 += dT1[j] * V[4 * j + 2];
+    }
+    float dt[3];
+    dt[0] = xmask * (dJ02 * (-fx / tz2));
+    dt[1] = ymask * (dJ12 * (-fy / tz2));
+    dt[2] = dJ00 * (-fx / tz2) + dJ11 * (-fy / tz2) + dJ02 * (2.f * fx * tx / tz3) +
+            dJ12 * (2.f * fy * ty / tz3) + acc[9];  // + d/d depth (depth = view z)
+    for (int j = 0; j < 3; ++j) dmean[j] = V[4 * j + 0] * dt[0] + V[4 * j + 1] * dt[1] + V[4 * j + 2] * dt[2];
+
+    // ---- projection: NDC = hom.xy / (hom.w + 1e-7) -------------------------------
+    {
+      const float hx = P[0] * px + P[4] * py + P[8] * pz + P[12];
+      const float hy = P[1] * px + P[5] * py + P[9] * pz + P[13];
+      const float hw = P[3] * px + P[7] * py + P[11] * pz + P[15];
+      const float wi = 1.f / (hw + 0.0000001f);
+      const float wi2 = wi * wi;
+      for (int j = 0; j < 3; ++j) {
+        dmean[j] += dndc_x * (P[4 * j + 0] * wi - hx * wi2 * P[4 * j + 3]) +
+                    dndc_y * (P[4 * j + 1] * wi - hy * wi2 * P[4 * j + 3]);
+      }
+    }
+
+    // ---- SH colour ----------------------------------------------------------------
+    if (a.g.shs) {
+      const uint8_t cl = a.geom.clamped[idx];
+      const float g0 = (cl & 1) ? 0.f : dcol[0];
+      const float g1 = (cl & 2) ? 0.f : dcol[1];
+      const float g2 = (cl & 4) ? 0.f : dcol[2];
+      const float cx = __ldg(sd.campos + 0), cy = __ldg(sd.campos + 1), cz = __ldg(sd.campos + 2);
+      const float ddx = px - cx, ddy = py - cy, ddz = pz - cz;
+      const float len = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
+      const float x = ddx / len, y = ddy / len, z = ddz / len;
+      float gdx, gdy, gdz;
+      sh_backward(sd.sh_degree, M, a.g.shs + (size_t)idx * 3 * M, g0, g1, g2, x, y, z,
+                  (!pose_only && a.out.dL_dsh) ? a.out.dL_dsh + (size_t)idx * 3 * M : nullptr, gdx, gdy, gdz);
+      // d/d(unnormalised direction) = (g - dir (dir . g)) / |d|
+      const float dotv = x * gdx + y * gdy + z * gdz;
+      dmean[0] += (gdx - x * dotv) / len;
+      dmean[1] += (gdy - y * dotv) / len;
+      dmean[2] += (gdz - z * dotv) / len;
+    }
+    if (!pose_only) {
+      for (int j = 0; j < 3; ++j) a.out.dL_dmeans3D[3 * idx + j] = dmean[j];
+
+      // ---- 3D covariance -> scale and rotation ----------------------------------
+      if (!a.g.cov3D_precomp) {
+        const float s3[3] = {sx, sy, sz};
+        float Mm[9];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) Mm[3 * i + j] = R[3 * i + j] * s3[j];
+        // symmetric matrix-entry derivative: diagonal = dcov, off-diagonal = dcov / 2
+        const float G[9] = {dcov[0], 0.5f * dcov[1], 0.5f * dcov[2], 0.5f * dcov[1], dcov[3],
+                            0.5f * dcov[4], 0.5f * dcov[2], 0.5f * dcov[4], dcov[5]};
+        float dM[9];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j)
+            dM[3 * i + j] = 2.f * (G[3 * i] * Mm[j] + G[3 * i + 1] * Mm[3 + j] + G[3 * i + 2] * Mm[6 + j]);
+        float dR[9];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) dR[3 * i + j] = dM[3 * i + j] * s3[j];
+        for (int j = 0; j < 3; ++j) {
+          const float ds = dM[j] * R[j] + dM[3 + j] * R[3 + j] + dM[6 + j] * R[6 + j];
+          a.out.dL_dscales[3 * idx + j] = ds * mod;
+        }
+        const float r = qr, x = qx, y = qy, z = qz;
+        float4 dq;
+        dq.x = 2.f * (-z * dR[1] + y * dR[2] + z * dR[3] - x * dR[5] - y * dR[6] + x * dR[7]);
+        dq.y = 2.f * (y * dR[1] + z * dR[2] + y * dR[3] - 2.f * x * dR[4] - r * dR[5] + z * dR[6] + r * dR[7] -
+                      2.f * x * dR[8]);
+        dq.z = 2.f * (-2.f * y * dR[0] + x * dR[1] + r * dR[2] + x * dR[3] + z * dR[5] - r * dR[6] + z * dR[7] -
+                      2.f * y * dR[8]);
+        dq.w = 2.f * (-2.f * z * dR[0] - r * dR[1] + x * dR[2] + r * dR[3] - 2.f * z * dR[4] + y * dR[5] +
+                      x * dR[6] + y * dR[7]);
+        if ((((uintptr_t)a.out.dL_drotations) & 15) == 0) {
+          reinterpret_cast<float4*>(a.out.dL_drotations)[idx] = dq;
+        } else {
+          a.out.dL_drotations[4 * idx + 0] = dq.x;
+          a.out.dL_drotations[4 * idx + 1] = dq.y;
+          a.out.dL_drotations[4 * idx + 2] = dq.z;
+          a.out.dL_drotations[4 * idx + 3] = dq.w;
+        }
+      }
+      return;
+    }
+  }
+  if (!pose_only) return;
+  // ---- pose-only form: the block's SE(3) gradient terms in float64 -----------------
+  double term[6] = {0, 0, 0, 0, 0, 0};
+  if (nt > 0 && sd.pose) {
+    const double* R64 = sd.pose->R64;
+    const double p0 = a.g.means3D[3 * idx], p1 = a.g.means3D[3 * idx + 1], p2 = a.g.means3D[3 * idx + 2];
+    const double g0 = dmean[0], g1 = dmean[1], g2 = dmean[2];
+    const double q0 = R64[0] * p0 + R64[1] * p1 + R64[2] * p2;
+    const double q1 = R64[3] * p0 + R64[4] * p1 + R64[5] * p2;
+    const double q2 = R64[6] * p0 + R64[7] * p1 + R64[8] * p2;
+    term[0] = g0;
+    term[1] = g1;
+    term[2] = g2;
+    term[3] = q1 * g2 - q2 * g1;
+    term[4] = q2 * g0 - q0 * g2;
+    term[5] = q0 * g1 - q1 * g0;
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double vv = term[k];
+    for (int o = 16; o > 0; o >>= 1) vv += __shfl_xor_sync(0xffffffffu, vv, o);
+    if (lane == 0) s_red[warp][k] = vv;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double vv = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) vv += s_red[w][threadIdx.x];
+    a.pose_partials[(size_t)blockIdx.x * 9 + threadIdx.x] = vv;
+  } else if (threadIdx.x < 9) {
+    a.pose_partials[(size_t)blockIdx.x * 9 + threadIdx.x] = 0.0;
+  }
+}
+
+template <class Scenes>
+void launch_preprocess_bwd(const PreBwdArgs<Scenes>& a, int blocks, cudaStream_t st) {
+  k_preprocess_bwd<Scenes><<<blocks, 256, 0, st>>>(a);
+}
+template void launch_preprocess_bwd<SingleScene>(const PreBwdArgs<SingleScene>&, int, cudaStream_t);
+template void launch_preprocess_bwd<SceneTable>(const PreBwdArgs<SceneTable>&, int, cudaStream_t);
+
+}  // namespace cfgs

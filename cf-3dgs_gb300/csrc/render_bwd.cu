@@ -1,0 +1,371 @@
+// Backward, part 1: the per-tile render backward with in-block gradient reduction,
+// and the backward entry points (the per-Gaussian part is in preprocess_bwd.cu).
+//
+// Upstream accumulates every (pixel, Gaussian) gradient with a global atomicAdd.
+// Here each tile reduces the gradients of its 256 pixels per instance inside the
+// block (a transposing warp reduction, then a fixed-order sum over the 8 warps) and
+// writes one 48-byte record per (Gaussian, tile) instance, at the instance's
+// pre-sort index. A Gaussian's instances are contiguous in pre-sort order, so the
+// preprocess backward sums its records in a fixed order: no atomics, bit-identical
+// results run to run.
+#include <mutex>
+
+#include "cfgs_internal.cuh"
+#include "kernels.cuh"
+
+namespace cfgs {
+
+constexpr int kBwdBatch = 64;
+constexpr int kWarps = kTilePixels / 32;
+
+// Sums 16 per-lane values across the warp in 16 shuffles (instead of 80): each step
+// halves the number of values a lane carries. On return lane L holds the warp total
+// of value index L >> 1.
+__device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lane) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    bool up = lane & 16;
+    float send = up ? v[k] : v[k + 8];
+    float keep = up ? v[k + 8] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    bool up = lane & 8;
+    float send = up ? v[k] : v[k + 4];
+    float keep = up ? v[k + 4] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    bool up = lane & 4;
+    float send = up ? v[k] : v[k + 2];
+    float keep = up ? v[k + 2] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  {
+    bool up = lane & 2;
+    float send = up ? v[0] : v[1];
+    float keep = up ? v[1] : v[0];
+    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+  return v[0];
+}
+
+// d/dc of mean |clamp(c, 0, 1) - t| as autograd forms it.
+__device__ __forceinline__ float l1_grad(float c, float t, float inv_numel) {
+  float d = fminf(fmaxf(c, 0.0f), 1.0f) - t;
+  float sgn = d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f);
+  return (c >= 0.0f && c <= 1.0f) ? inv_numel * sgn : 0.0f;
+}
+
+// Same pixel boxes and exact shortcuts as the forward (box_may_contribute per warp and
+// instance, alpha_threshold per pixel); the cross-warp sum of an instance adds only the
+// warps that kept it (the others' terms are exact zeros).
+template <class Scenes>
+__global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes> a) {
+  __shared__ float4 s_xyt[kBwdBatch];
+  __shared__ float4 s_co[kBwdBatch];
+  __shared__ float4 s_rgbd[kBwdBatch];
+  __shared__ uint32_t s_pidx[kBwdBatch];
+  __shared__ float s_part[kWarps][kBwdBatch][10];
+  __shared__ uint32_t s_keep[kWarps][kBwdBatch / 32];
+  __shared__ uint32_t s_max;
+  if ((int64_t)a.counts->num_rendered > a.cap) return;
+  const int tile = blockIdx.x;
+  const SceneDesc& sd = a.scenes.for_tile(tile);
+  const int lt = tile - sd.tile_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int bx0 = (lt % sd.grid_x) * kTileX + (warp & 1) * 8;
+  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 4;
+  const int px = bx0 + (lane & 7), py = by0 + (lane >> 3);
+  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 3);
+  const bool inside = px < sd.W && py < sd.H;
+  const float pxf = (float)px, pyf = (float)py;
+  const uint32_t lo = a.tile_range[tile];
+  const int n = (int)(a.tile_range[tile + 1] - lo);
+  const size_t HW = (size_t)sd.W * sd.H;
+  const size_t pix = inside ? (size_t)py * sd.W + px : 0;
+  const size_t gp = (size_t)sd.pix_base + pix;
+
+  float T_final = 1.0f, dC0 = 0.f, dC1 = 0.f, dC2 = 0.f, dD = 0.f, dA = 0.f;
+  uint32_t last = 0;
+  if (inside) {
+    T_final = a.final_T[gp];
+    last = a.n_contrib[gp];
+    const size_t cb = 3 * (size_t)sd.pix_base + pix;
+    if (a.target) {
+      dC0 = l1_grad(a.color[cb], a.target[cb], sd.inv_numel);
+      dC1 = l1_grad(a.color[cb + HW], a.target[cb + HW], sd.inv_numel);
+      dC2 = l1_grad(a.color[cb + 2 * HW], a.target[cb + 2 * HW], sd.inv_numel);
+    } else {
+      dC0 = a.dL_dcolor[cb];
+      dC1 = a.dL_dcolor[cb + HW];
+      dC2 = a.dL_dcolor[cb + 2 * HW];
+      if (a.dL_ddepth) dD = a.dL_ddepth[gp];
+      if (a.dL_dalpha) dA = a.dL_dalpha[gp];
+    }
+  }
+  if (threadIdx.x == 0) s_max = 0;
+  __syncthreads();
+  if (last) atomicMax(&s_max, last);
+  __syncthreads();
+  const int max_last = (int)s_max;
+  const float bg_dot = __ldg(sd.bg + 0) * dC0 + __ldg(sd.bg + 1) * dC1 + __ldg(sd.bg + 2) * dC2;
+
+  float T = T_final;
+  float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, accd = 0.f;
+  float last_a = 0.f, last0 = 0.f, last1 = 0.f, last2 = 0.f, lastd = 0.f;
+
+  const int nb = (max_last + kBwdBatch - 1) / kBwdBatch;
+  for (int b = nb - 1; b >= 0; --b) {
+    const int base = b * kBwdBatch;
+    const int cnt = min(kBwdBatch, max_last - base);
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      uint32_t i = lo + base + threadIdx.x;
+      uint32_t g = a.sorted_gid[i];
+      s_pidx[threadIdx.x] = a.sorted_pidx[i];
+      float2 m = a.xy[g];
+      float4 co = a.conic_op[g];
+      s_xyt[threadIdx.x] = make_float4(m.x, m.y, alpha_threshold(co.w), 0.0f);
+      s_co[threadIdx.x] = make_float4(-0.5f * co.x, -co.y, -0.5f * co.z, co.w);
+      s_rgbd[threadIdx.x] = a.rgbd[g];
+    }
+    __syncthreads();
+    uint32_t keep[kBwdBatch / 32];
+#pragma unroll
+    for (int r = 0; r < kBwdBatch / 32; ++r) {
+      const int j = r * 32 + lane;
+      bool k = false;
+      if (j < cnt) {
+        const float4 xyt = s_xyt[j];
+        const float4 co = s_co[j];
+        k = box_may_contribute(make_float2(xyt.x, xyt.y), co.x, co.y, co.z, xyt.z, bxf0, bxf1, byf0, byf1);
+      }
+      keep[r] = __ballot_sync(0xffffffffu, k);
+      if (lane == 0) s_keep[warp][r] = keep[r];
+    }
+#pragma unroll
+    for (int r = kBwdBatch / 32 - 1; r >= 0; --r) {
+     uint32_t mk = keep[r];
+     while (mk) {
+      const int bit = 31 - __clz(mk);
+      mk &= ~(1u << bit);
+      const int j = r * 32 + bit;
+      const int c = base + j;
+      float v[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) v[k] = 0.f;
+      bool contrib = false;
+      if (c < (int)last) {
+        const float4 m = s_xyt[j];
+        float4 co = s_co[j];
+        float dx = m.x - pxf, dy = m.y - pyf;
+        float power = gauss_power(co.x, co.y, co.z, dx, dy);
+        if (!(power > 0.0f || power < m.z)) {
+          float G = exp_ref_inrange(power);
+          float alpha = fminf(CFGS_ALPHA_MAX, co.w * G);
+          if (alpha >= CFGS_ALPHA_MIN) {
+            contrib = true;
+            float4 col = s_rgbd[j];
+            float one_m = 1.0f - alpha;
+            T = T / one_m;
+            float w = alpha * T;
+            v[6] = dC0 * w;
+            v[7] = dC1 * w;
+            v[8] = dC2 * w;
+            v[9] = dD * w;
+            acc0 = last_a * last0 + (1.f - last_a) * acc0;
+            acc1 = last_a * last1 + (1.f - last_a) * acc1;
+            acc2 = last_a * last2 + (1.f - last_a) * acc2;
+            accd = last_a * lastd + (1.f - last_a) * accd;
+            last0 = col.x;
+            last1 = col.y;
+            last2 = col.z;
+            lastd = col.w;
+            last_a = alpha;
+            float dLda = (col.x - acc0) * dC0 + (col.y - acc1) * dC1 + (col.z - acc2) * dC2 +
+                         (col.w - accd) * dD;
+            dLda *= T;
+            float tf = T_final / one_m;
+            dLda += tf * (dA - bg_dot);
+            v[5] = G * dLda;                 // d/d opacity (straight through the 0.99 clamp)
+            float dLdp = G * (co.w * dLda);  // d/d power
+            // power = ca dx^2 + cb dx dy + cc dy^2, dx = mean.x - pixel.x
+            v[0] = dLdp * (2.f * co.x * dx + co.y * dy);
+            v[1] = dLdp * (2.f * co.z * dy + co.y * dx);
+            v[2] = -0.5f * dx * dx * dLdp;  // d/d conic.a
+            v[3] = -dx * dy * dLdp;         // d/d conic.b
+            v[4] = -0.5f * dy * dy * dLdp;  // d/d conic.c
+          }
+        }
+      }
+      if (__ballot_sync(0xffffffffu, contrib)) {
+        float r = warp_transpose_reduce16(v, lane);
+        int k = lane >> 1;
+        if (!(lane & 1) && k < 10) s_part[warp][j][k] = r;
+      } else if (lane < 10) {
+        s_part[warp][j][lane] = 0.f;
+      }
+     }
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      const int j = threadIdx.x;
+      float sum[10];
+#pragma unroll
+      for (int k = 0; k < 10; ++k) sum[k] = 0.f;
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w)
+        if ((s_keep[w][j >> 5] >> (j & 31)) & 1u)
+#pragma unroll
+          for (int k = 0; k < 10; ++k) sum[k] += s_part[w][j][k];
+      float4* rec = a.records + (size_t)kRecordFloat4 * s_pidx[threadIdx.x];
+      rec[0] = make_float4(sum[0], sum[1], sum[2], sum[3]);
+      rec[1] = make_float4(sum[4], sum[5], sum[6], sum[7]);
+      rec[2] = make_float4(sum[8], sum[9], 0.f, 0.f);
+    }
+  }
+  for (int i = max_last + threadIdx.x; i < n; i += blockDim.x) {
+    float4* rec = a.records + (size_t)kRecordFloat4 * a.sorted_pidx[lo + i];
+    rec[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    rec[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    rec[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+template <class Scenes>
+void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st) {
+  k_render_bwd<Scenes><<<tiles, kTilePixels, 0, st>>>(a);
+}
+template void launch_render_bwd<SingleScene>(const RenderBwdArgs<SingleScene>&, int, cudaStream_t);
+template void launch_render_bwd<SceneTable>(const RenderBwdArgs<SceneTable>&, int, cudaStream_t);
+
+}  // namespace cfgs
+
+using namespace cfgs;
+
+extern "C" int cfgs_render_backward(const CfgsSettings* s, int32_t num_gaussians, const void* geom, const void* image,
+                                    const void* binning, int64_t capacity, void* scratch, const float* dL_dcolor,
+                                    const float* dL_ddepth, const float* dL_dalpha, void* stream) {
+  if (!s || !geom || !image || !binning || !scratch || !dL_dcolor || !s->bg || num_gaussians < 0)
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if (s->image_width <= 0 || s->image_height <= 0) return CFGS_ERR_INVALID_ARGUMENT;
+  if (capacity < 0 || capacity > 0x7fffffffll) return CFGS_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  ImageLayout IL(s->image_width, s->image_height);
+  ImageView iv(const_cast<void*>(image), s->image_width, s->image_height);
+  GeomView gv(const_cast<void*>(geom), num_gaussians);
+  BinningView bv(const_cast<void*>(binning), capacity);
+  RenderBwdArgs<SingleScene> ra;
+  ra.scenes.d = single_scene_desc(s, num_gaussians, 0);
+  ra.tile_range = iv.tile_range;
+  ra.sorted_gid = bv.sorted_gid;
+  ra.sorted_pidx = bv.sorted_pidx;
+  ra.xy = gv.xy;
+  ra.conic_op = gv.conic_op;
+  ra.rgbd = gv.rgbd;
+  ra.final_T = iv.final_T;
+  ra.n_contrib = iv.n_contrib;
+  ra.dL_dcolor = dL_dcolor;
+  ra.dL_ddepth = dL_ddepth;
+  ra.dL_dalpha = dL_dalpha;
+  ra.color = nullptr;
+  ra.target = nullptr;
+  ra.records = static_cast<float4*>(scratch);
+  ra.cap = capacity;
+  ra.counts = iv.counts;
+  launch_render_bwd(ra, IL.num_tiles, st);
+  CFGS_CHECK_LAUNCH(s->debug, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_preprocess_backward(const CfgsSettings* s, const CfgsGaussians* g, const int32_t* radii,
+                                        const void* geom, const void* image, int64_t capacity, const void* scratch,
+                                        const CfgsGradients* out, void* stream) {
+  if (!s || !g || !geom || !image || !scratch || !out || !s->viewmatrix || !s->projmatrix)
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if (g->num_gaussians == 0) return CFGS_OK;
+  if (g->num_gaussians < 0 || !radii || !g->means3D || !g->opacities) return CFGS_ERR_INVALID_ARGUMENT;
+  if (!out->dL_dmeans2D || !out->dL_dcolors || !out->dL_dopacity || !out->dL_dmeans3D || !out->dL_dcov3D)
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if (!g->cov3D_precomp && (!out->dL_dscales || !out->dL_drotations || !g->scales || !g->rotations))
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if ((g->shs == nullptr) == (g->colors_precomp == nullptr)) return CFGS_ERR_INVALID_ARGUMENT;
+  if (g->shs && !s->campos) return CFGS_ERR_INVALID_ARGUMENT;
+  if (capacity < 0 || capacity > 0x7fffffffll) return CFGS_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  ImageView iv(const_cast<void*>(image), s->image_width, s->image_height);
+  PreBwdArgs<SingleScene> pa;
+  pa.scenes.d = single_scene_desc(s, g->num_gaussians, g->sh_coeffs);
+  pa.g = *g;
+  pa.radii = radii;
+  pa.geom = GeomView(const_cast<void*>(geom), g->num_gaussians);
+  pa.records = static_cast<const float4*>(scratch);
+  pa.out = *out;
+  pa.total_slots = g->num_gaussians;
+  pa.cap = capacity;
+  pa.counts = iv.counts;
+  pa.pose_partials = nullptr;
+  launch_preprocess_bwd(pa, div_up(g->num_gaussians, 256), st);
+  CFGS_CHECK_LAUNCH(s->debug, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_backward(const CfgsSettings* s, const CfgsGaussians* g, const int32_t* radii, const void* geom,
+                             const void* image, const void* binning, int64_t capacity, void* scratch,
+                             const float* dL_dcolor, const float* dL_ddepth, const float* dL_dalpha,
+                             const CfgsGradients* out, void* stream) {
+  if (!g) return CFGS_ERR_INVALID_ARGUMENT;
+  if (g->num_gaussians == 0) return CFGS_OK;
+  int st = cfgs_render_backward(s, g->num_gaussians, geom, image, binning, capacity, scratch, dL_dcolor, dL_ddepth,
+                                dL_dalpha, stream);
+  if (st != CFGS_OK) return st;
+  return cfgs_preprocess_backward(s, g, radii, geom, image, capacity, scratch, out, stream);
+}
+
+// ---- allocation-free backward ----------------------------------------------------
+// Some callers cannot allocate device memory when they call the rasteriser: plugin
+// hosts that hand a plugin only its input and output buffers, and services that must
+// not allocate once they are serving. This entry point runs the same two kernels as
+// cfgs_backward, but the per-instance gradient records live in the fixed array below
+// instead of a caller-provided scratch buffer. Every GPU that loads this library holds
+// the array (30 MiB) until the process exits.
+static __device__ __align__(256) float4 g_noalloc_records[(size_t)CFGS_NOALLOC_MAX_INSTANCES * kRecordFloat4];
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// Device address of g_noalloc_records on the current device. The host-side name of
+// the array is only a stand-in, so the address is looked up once per device, with
+// that device current, and cached.
+int noalloc_records(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) return CFGS_ERR_LAUNCH;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_records) != cudaSuccess || p == nullptr) return CFGS_ERR_LAUNCH;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return CFGS_OK;
+}
+}  // namespace
+
+extern "C" int cfgs_backward_noalloc(const CfgsSettings* s, const CfgsGaussians* g, const int32_t* radii,
+                                     const void* geom, const void* image, const void* binning, int64_t capacity,
+                                     const float* dL_dcolor, const float* dL_ddepth, const float* dL_dalpha,
+                                     const CfgsGradients* out, void* stream) {
+  if (capacity < 0) return CFGS_ERR_INVALID_ARGUMENT;
+  if (capacity > CFGS_NOALLOC_MAX_INSTANCES) return CFGS_ERR_TOO_LARGE;
+  void* records = nullptr;
+  int st = noalloc_records(&records);
+  if (st != CFGS_OK) return st;
+  return cfgs_backward(s, g, radii, geom, image, binning, capacity, records, dL_dcolor, dL_ddepth, dL_dalpha, out,
+                       stream);
+}
