@@ -15,7 +15,7 @@
 
 namespace cfgs {
 
-constexpr int kBwdBatch = 64;
+constexpr int kBwdBatch = 128;
 constexpr int kWarps = kTilePixels / 32;
 
 // Sums 16 per-lane values across the warp in 16 shuffles (instead of 80): each step
@@ -170,8 +170,8 @@ __global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes
           if (alpha >= CFGS_ALPHA_MIN) {
             contrib = true;
             float4 col = s_rgbd[j];
-            float one_m = 1.0f - alpha;
-            T = T / one_m;
+            const float inv_one_m = __frcp_rn(1.0f - alpha);
+            T = T * inv_one_m;
             float w = alpha * T;
             v[6] = dC0 * w;
             v[7] = dC1 * w;
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes
             float dLda = (col.x - acc0) * dC0 + (col.y - acc1) * dC1 + (col.z - acc2) * dC2 +
                          (col.w - accd) * dD;
             dLda *= T;
-            float tf = T_final / one_m;
+            float tf = T_final * inv_one_m;
             dLda += tf * (dA - bg_dot);
             v[5] = G * dLda;                 // d/d opacity (straight through the 0.99 clamp)
             float dLdp = G * (co.w * dLda);  // d/d power

@@ -156,24 +156,121 @@ __device__ __forceinline__ int merge_split(const uint64_t* A, int la, const uint
   return lo;
 }
 
+// Stable LSD radix sort of a tile segment (n <= kSortCap) by the 32-bit depth bits,
+// 4 bits per pass, in shared memory: each thread owns a run of consecutive elements,
+// counts its digits into its own column of a [16][256] table, a block-wide exclusive
+// scan of the table in digit-major order gives every (digit, thread) its first output
+// slot, and the thread writes its elements in order (stable). Passes whose digit is the
+// same for all elements are skipped. Equal depths then appear in input order, which the
+// scatter left arbitrary, so each run of equal depths is re-sorted by pre-sort index:
+// the final order is (depth, pre-sort index), unique.
+struct RadixSmem {
+  uint32_t key[2][kSortCap];
+  uint16_t idx[2][kSortCap];
+  uint32_t cnt[16][kSortThreads + 1];
+  uint32_t warp_tot[kSortThreads / 32];
+  int trivial;
+};
+
+__device__ void radix_sort_segment(RadixSmem& S, const uint64_t* keys, int n, int& out_buf) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int E = (n + kSortThreads - 1) / kSortThreads;
+  const int b0 = min(n, t * E), b1 = min(n, b0 + E);
+  for (int i = t; i < n; i += kSortThreads) {
+    S.key[0][i] = (uint32_t)(keys[i] >> 32);
+    S.idx[0][i] = (uint16_t)i;
+  }
+  int cur = 0;
+  for (int shift = 0; shift < 32; shift += 4) {
+#pragma unroll
+    for (int d = 0; d < 16; ++d) S.cnt[d][t] = 0;
+    __syncthreads();
+    for (int i = b0; i < b1; ++i) S.cnt[(S.key[cur][i] >> shift) & 15u][t]++;
+    __syncthreads();
+    // exclusive scan of cnt in digit-major order; thread t owns flat entries [16t, 16t+16)
+    uint32_t loc[16];
+    uint32_t run = 0;
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int f = 16 * t + u;
+      loc[u] = run;
+      run += S.cnt[f >> 8][f & 255];
+    }
+    uint32_t x = run;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) S.warp_tot[warp] = x;
+    __syncthreads();
+    uint32_t pre = x - run;
+    for (int w = 0; w < warp; ++w) pre += S.warp_tot[w];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int f = 16 * t + u;
+      S.cnt[f >> 8][f & 255] = pre + loc[u];
+    }
+    __syncthreads();
+    bool trivial = false;  // one digit holds every element: the pass changes nothing
+#pragma unroll
+    for (int d = 0; d < 16; ++d) {
+      const uint32_t start = S.cnt[d][0], end = d < 15 ? S.cnt[d + 1][0] : (uint32_t)n;
+      trivial |= (end - start == (uint32_t)n);
+    }
+    if (trivial) {  // uniform: every thread read the same bucket starts
+      __syncthreads();
+      continue;
+    }
+    const int nxt = cur ^ 1;
+    for (int i = b0; i < b1; ++i) {
+      const uint32_t k = S.key[cur][i];
+      const uint32_t pos = S.cnt[(k >> shift) & 15u][t]++;
+      S.key[nxt][pos] = k;
+      S.idx[nxt][pos] = S.idx[cur][i];
+    }
+    __syncthreads();
+    cur = nxt;
+  }
+  // runs of equal depth: insertion sort by pre-sort index (the key's low 32 bits)
+  for (int i = t; i < n; i += kSortThreads) {
+    const uint32_t k = S.key[cur][i];
+    const bool start = (i == 0 || S.key[cur][i - 1] != k) && (i + 1 < n && S.key[cur][i + 1] == k);
+    if (!start) continue;
+    int e = i + 1;
+    while (e < n && S.key[cur][e] == k) ++e;
+    for (int p = i + 1; p < e; ++p) {
+      const uint16_t v = S.idx[cur][p];
+      const uint32_t pv = (uint32_t)keys[v];
+      int q = p - 1;
+      while (q >= i && (uint32_t)keys[S.idx[cur][q]] > pv) {
+        S.idx[cur][q + 1] = S.idx[cur][q];
+        --q;
+      }
+      S.idx[cur][q + 1] = v;
+    }
+  }
+  __syncthreads();
+  out_buf = cur;
+}
+
 // One block per tile (global tile index: scene-agnostic). Segments of at most kSortCap
-// instances: bitonic sort in shared memory. Larger segments: bitonic-sort kSortCap
-// chunks, then merge them pairwise (merge path, ping-pong between keys and keys_alt)
-// inside the block.
+// instances: radix sort in shared memory (above). Larger segments: bitonic-sort
+// kSortCap chunks, then merge them pairwise (merge path, ping-pong between keys and
+// keys_alt) inside the block.
 __global__ void __launch_bounds__(kSortThreads) k_tile_sort(SortArgs a) {
-  __shared__ uint64_t s[kSortCap];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* s = reinterpret_cast<uint64_t*>(smem_raw);
   if ((int64_t)a.counts->num_rendered > a.cap) return;
   const uint32_t lo = a.tile_range[blockIdx.x];
   const int n = (int)(a.tile_range[blockIdx.x + 1] - lo);
   if (n == 0) return;
   uint64_t* keys = a.bin.keys + lo;
   if (n <= kSortCap) {
-    int n2 = next_pow2(n);
-    for (int i = threadIdx.x; i < n2; i += blockDim.x) s[i] = i < n ? keys[i] : ~0ull;
-    __syncthreads();
-    bitonic_sort_smem(s, n2);
+    RadixSmem& S = *reinterpret_cast<RadixSmem*>(smem_raw);
+    int buf = 0;
+    radix_sort_segment(S, keys, n, buf);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      uint32_t pidx = (uint32_t)s[i];
+      uint32_t pidx = (uint32_t)keys[S.idx[buf][i]];
       a.bin.sorted_pidx[lo + i] = pidx;
       a.bin.sorted_gid[lo + i] = a.bin.inst_gid[pidx];
     }
@@ -329,7 +426,14 @@ void launch_scatter(const ScatterArgs<Scenes>& a, int blocks, cudaStream_t st) {
   k_scatter<Scenes><<<blocks, kPreprocessBlock, 0, st>>>(a);
 }
 void launch_tile_sort(const SortArgs& a, int tiles, cudaStream_t st) {
-  k_tile_sort<<<tiles, kSortThreads, 0, st>>>(a);
+  constexpr size_t kSmem = sizeof(RadixSmem) > sizeof(uint64_t) * kSortCap ? sizeof(RadixSmem)
+                                                                          : sizeof(uint64_t) * kSortCap;
+  static bool attr_set = false;  // a function attribute: set once per process (before any capture)
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_tile_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+    attr_set = true;
+  }
+  k_tile_sort<<<tiles, kSortThreads, kSmem, st>>>(a);
 }
 template <class Scenes>
 void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st) {
