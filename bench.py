@@ -134,17 +134,17 @@ def _peaks() -> dict:
         return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu
+# captures summarised in profiles/<kernel>_1M_1080p.md, at the instance count K they were
+# taken at; scaled by instances for another K.
+NCU_TRAFFIC = {"render_bwd": (300232960 + 630901760, 12433348)}
+
+
 def _traffic(kernel: str, K: int):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, scaled to this
-    launch by instance count when the capture was taken on a smaller case."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
-    try:
-        with open(path) as f:
-            d = json.load(f)
-        e = d[kernel]
-        return e["bytes_per_launch"] * (K / e["num_rendered"]) if e.get("scale_by_instances") else e["bytes_per_launch"]
-    except Exception:
+    if kernel not in NCU_TRAFFIC:
         return None
+    b, k0 = NCU_TRAFFIC[kernel]
+    return int(b * K / k0)
 
 
 # ---------------------------------------------------------------------------

@@ -3,7 +3,7 @@
 //
 // Upstream accumulates every (pixel, Gaussian) gradient with a global atomicAdd.
 // Here each tile reduces the gradients of its 256 pixels per instance inside the
-// block (a transposing warp reduction, then a fixed-order sum over the 8 warps) and
+// block (a transposing warp reduction, then a fixed-order sum over the 4 warps) and
 // writes one 48-byte record per (Gaussian, tile) instance, at the instance's
 // pre-sort index. A Gaussian's instances are contiguous in pre-sort order, so the
 // preprocess backward sums its records in a fixed order: no atomics, bit-identical
@@ -16,7 +16,8 @@
 namespace cfgs {
 
 constexpr int kBwdBatch = 128;
-constexpr int kWarps = kTilePixels / 32;
+constexpr int kBwdThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
+constexpr int kWarps = kBwdThreads / 32;
 
 // Sums 16 per-lane values across the warp in 16 shuffles (instead of 80): each step
 // halves the number of values a lane carries. On return lane L holds the warp total
@@ -60,11 +61,96 @@ __device__ __forceinline__ float l1_grad(float c, float t, float inv_numel) {
   return (c >= 0.0f && c <= 1.0f) ? inv_numel * sgn : 0.0f;
 }
 
-// Same pixel boxes and exact shortcuts as the forward (box_may_contribute per warp and
-// instance, alpha_threshold per pixel); the cross-warp sum of an instance adds only the
-// warps that kept it (the others' terms are exact zeros).
+// Back-to-front state of one pixel: its upstream gradients, the transmittance being
+// unwound and the running colour/depth behind the current instance.
+struct PixelBwd {
+  float T_final, dC0, dC1, dC2, dD, dA, bg_dot;
+  float T, acc0, acc1, acc2, accd, last_a, last0, last1, last2, lastd;
+  uint32_t last;
+};
+
+// Loads pixel pix's forward state and upstream gradient (zeros outside the image).
 template <class Scenes>
-__global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes> a) {
+__device__ __forceinline__ void load_pixel(PixelBwd& p, const RenderBwdArgs<Scenes>& a, const SceneDesc& sd,
+                                           bool inside, size_t pix) {
+  const size_t HW = (size_t)sd.W * sd.H;
+  const size_t gp = (size_t)sd.pix_base + pix;
+  p.T_final = 1.0f;
+  p.dC0 = p.dC1 = p.dC2 = p.dD = p.dA = 0.f;
+  p.last = 0;
+  if (inside) {
+    p.T_final = a.final_T[gp];
+    p.last = a.n_contrib[gp];
+    const size_t cb = 3 * (size_t)sd.pix_base + pix;
+    if (a.target) {
+      p.dC0 = l1_grad(a.color[cb], a.target[cb], sd.inv_numel);
+      p.dC1 = l1_grad(a.color[cb + HW], a.target[cb + HW], sd.inv_numel);
+      p.dC2 = l1_grad(a.color[cb + 2 * HW], a.target[cb + 2 * HW], sd.inv_numel);
+    } else {
+      p.dC0 = a.dL_dcolor[cb];
+      p.dC1 = a.dL_dcolor[cb + HW];
+      p.dC2 = a.dL_dcolor[cb + 2 * HW];
+      if (a.dL_ddepth) p.dD = a.dL_ddepth[gp];
+      if (a.dL_dalpha) p.dA = a.dL_dalpha[gp];
+    }
+  }
+  p.bg_dot = __ldg(sd.bg + 0) * p.dC0 + __ldg(sd.bg + 1) * p.dC1 + __ldg(sd.bg + 2) * p.dC2;
+  p.T = p.T_final;
+  p.acc0 = p.acc1 = p.acc2 = p.accd = 0.f;
+  p.last_a = p.last0 = p.last1 = p.last2 = p.lastd = 0.f;
+}
+
+// Unwinds one instance at list position c for one pixel and adds its ten gradient terms
+// (d mean2D x/y, d conic a/b/c, d opacity, d rgb, d depth) to v. Returns whether the
+// instance contributed to the pixel in the forward pass.
+__device__ __forceinline__ bool unwind_step(PixelBwd& p, int c, float pxf, float pyf, const float4& m,
+                                            const float4& co, const float4* s_rgbd, int j, float (&v)[16]) {
+  if (c >= (int)p.last) return false;
+  const float dx = m.x - pxf, dy = m.y - pyf;
+  const float power = gauss_power(co.x, co.y, co.z, dx, dy);
+  if (power > 0.0f || power < m.z) return false;
+  const float G = exp_ref_inrange(power);
+  const float alpha = fminf(CFGS_ALPHA_MAX, co.w * G);
+  if (alpha < CFGS_ALPHA_MIN) return false;
+  const float4 col = s_rgbd[j];
+  const float inv_one_m = __frcp_rn(1.0f - alpha);
+  p.T = p.T * inv_one_m;
+  const float w = alpha * p.T;
+  v[6] += p.dC0 * w;
+  v[7] += p.dC1 * w;
+  v[8] += p.dC2 * w;
+  v[9] += p.dD * w;
+  p.acc0 = p.last_a * p.last0 + (1.f - p.last_a) * p.acc0;
+  p.acc1 = p.last_a * p.last1 + (1.f - p.last_a) * p.acc1;
+  p.acc2 = p.last_a * p.last2 + (1.f - p.last_a) * p.acc2;
+  p.accd = p.last_a * p.lastd + (1.f - p.last_a) * p.accd;
+  p.last0 = col.x;
+  p.last1 = col.y;
+  p.last2 = col.z;
+  p.lastd = col.w;
+  p.last_a = alpha;
+  float dLda = (col.x - p.acc0) * p.dC0 + (col.y - p.acc1) * p.dC1 + (col.z - p.acc2) * p.dC2 + (col.w - p.accd) * p.dD;
+  dLda *= p.T;
+  const float tf = p.T_final * inv_one_m;
+  dLda += tf * (p.dA - p.bg_dot);
+  v[5] += G * dLda;                      // d/d opacity (straight through the 0.99 clamp)
+  const float dLdp = G * (co.w * dLda);  // d/d power
+  // power = ca dx^2 + cb dx dy + cc dy^2, dx = mean.x - pixel.x
+  v[0] += dLdp * (2.f * co.x * dx + co.y * dy);
+  v[1] += dLdp * (2.f * co.z * dy + co.y * dx);
+  v[2] += -0.5f * dx * dx * dLdp;  // d/d conic.a
+  v[3] += -dx * dy * dLdp;         // d/d conic.b
+  v[4] += -0.5f * dy * dy * dLdp;  // d/d conic.c
+  return true;
+}
+
+// One block of 128 threads per tile with the forward's pixel boxes (warp w: 8x8 box,
+// lane: rows r and r + 4) and exact shortcuts (box_may_contribute per warp and
+// instance, alpha_threshold per pixel). A lane adds its two pixels' terms before the
+// warp reduction; the cross-warp sum of an instance adds only the warps that kept it
+// (the others' terms are exact zeros).
+template <class Scenes>
+__global__ void __launch_bounds__(kBwdThreads) k_render_bwd(RenderBwdArgs<Scenes> a) {
   __shared__ float4 s_xyt[kBwdBatch];
   __shared__ float4 s_co[kBwdBatch];
   __shared__ float4 s_rgbd[kBwdBatch];
@@ -78,45 +164,23 @@ __global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes
   const int lt = tile - sd.tile_base;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int bx0 = (lt % sd.grid_x) * kTileX + (warp & 1) * 8;
-  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 4;
-  const int px = bx0 + (lane & 7), py = by0 + (lane >> 3);
-  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 3);
-  const bool inside = px < sd.W && py < sd.H;
-  const float pxf = (float)px, pyf = (float)py;
+  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 8;
+  const int px = bx0 + (lane & 7), py0 = by0 + (lane >> 3), py1 = py0 + 4;
+  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 7);
+  const bool in0 = px < sd.W && py0 < sd.H, in1 = px < sd.W && py1 < sd.H;
+  const float pxf = (float)px, pyf0 = (float)py0, pyf1 = (float)py1;
   const uint32_t lo = a.tile_range[tile];
   const int n = (int)(a.tile_range[tile + 1] - lo);
-  const size_t HW = (size_t)sd.W * sd.H;
-  const size_t pix = inside ? (size_t)py * sd.W + px : 0;
-  const size_t gp = (size_t)sd.pix_base + pix;
 
-  float T_final = 1.0f, dC0 = 0.f, dC1 = 0.f, dC2 = 0.f, dD = 0.f, dA = 0.f;
-  uint32_t last = 0;
-  if (inside) {
-    T_final = a.final_T[gp];
-    last = a.n_contrib[gp];
-    const size_t cb = 3 * (size_t)sd.pix_base + pix;
-    if (a.target) {
-      dC0 = l1_grad(a.color[cb], a.target[cb], sd.inv_numel);
-      dC1 = l1_grad(a.color[cb + HW], a.target[cb + HW], sd.inv_numel);
-      dC2 = l1_grad(a.color[cb + 2 * HW], a.target[cb + 2 * HW], sd.inv_numel);
-    } else {
-      dC0 = a.dL_dcolor[cb];
-      dC1 = a.dL_dcolor[cb + HW];
-      dC2 = a.dL_dcolor[cb + 2 * HW];
-      if (a.dL_ddepth) dD = a.dL_ddepth[gp];
-      if (a.dL_dalpha) dA = a.dL_dalpha[gp];
-    }
-  }
+  PixelBwd p0, p1;
+  load_pixel(p0, a, sd, in0, in0 ? (size_t)py0 * sd.W + px : 0);
+  load_pixel(p1, a, sd, in1, in1 ? (size_t)py1 * sd.W + px : 0);
   if (threadIdx.x == 0) s_max = 0;
   __syncthreads();
-  if (last) atomicMax(&s_max, last);
+  const uint32_t my_last = max(p0.last, p1.last);
+  if (my_last) atomicMax(&s_max, my_last);
   __syncthreads();
   const int max_last = (int)s_max;
-  const float bg_dot = __ldg(sd.bg + 0) * dC0 + __ldg(sd.bg + 1) * dC1 + __ldg(sd.bg + 2) * dC2;
-
-  float T = T_final;
-  float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, accd = 0.f;
-  float last_a = 0.f, last0 = 0.f, last1 = 0.f, last2 = 0.f, lastd = 0.f;
 
   const int nb = (max_last + kBwdBatch - 1) / kBwdBatch;
   for (int b = nb - 1; b >= 0; --b) {
@@ -149,67 +213,27 @@ __global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes
     }
 #pragma unroll
     for (int r = kBwdBatch / 32 - 1; r >= 0; --r) {
-     uint32_t mk = keep[r];
-     while (mk) {
-      const int bit = 31 - __clz(mk);
-      mk &= ~(1u << bit);
-      const int j = r * 32 + bit;
-      const int c = base + j;
-      float v[16];
+      uint32_t mk = keep[r];
+      while (mk) {
+        const int bit = 31 - __clz(mk);
+        mk &= ~(1u << bit);
+        const int j = r * 32 + bit;
+        const int c = base + j;
+        float v[16];
 #pragma unroll
-      for (int k = 0; k < 16; ++k) v[k] = 0.f;
-      bool contrib = false;
-      if (c < (int)last) {
+        for (int k = 0; k < 16; ++k) v[k] = 0.f;
         const float4 m = s_xyt[j];
-        float4 co = s_co[j];
-        float dx = m.x - pxf, dy = m.y - pyf;
-        float power = gauss_power(co.x, co.y, co.z, dx, dy);
-        if (!(power > 0.0f || power < m.z)) {
-          float G = exp_ref_inrange(power);
-          float alpha = fminf(CFGS_ALPHA_MAX, co.w * G);
-          if (alpha >= CFGS_ALPHA_MIN) {
-            contrib = true;
-            float4 col = s_rgbd[j];
-            const float inv_one_m = __frcp_rn(1.0f - alpha);
-            T = T * inv_one_m;
-            float w = alpha * T;
-            v[6] = dC0 * w;
-            v[7] = dC1 * w;
-            v[8] = dC2 * w;
-            v[9] = dD * w;
-            acc0 = last_a * last0 + (1.f - last_a) * acc0;
-            acc1 = last_a * last1 + (1.f - last_a) * acc1;
-            acc2 = last_a * last2 + (1.f - last_a) * acc2;
-            accd = last_a * lastd + (1.f - last_a) * accd;
-            last0 = col.x;
-            last1 = col.y;
-            last2 = col.z;
-            lastd = col.w;
-            last_a = alpha;
-            float dLda = (col.x - acc0) * dC0 + (col.y - acc1) * dC1 + (col.z - acc2) * dC2 +
-                         (col.w - accd) * dD;
-            dLda *= T;
-            float tf = T_final * inv_one_m;
-            dLda += tf * (dA - bg_dot);
-            v[5] = G * dLda;                 // d/d opacity (straight through the 0.99 clamp)
-            float dLdp = G * (co.w * dLda);  // d/d power
-            // power = ca dx^2 + cb dx dy + cc dy^2, dx = mean.x - pixel.x
-            v[0] = dLdp * (2.f * co.x * dx + co.y * dy);
-            v[1] = dLdp * (2.f * co.z * dy + co.y * dx);
-            v[2] = -0.5f * dx * dx * dLdp;  // d/d conic.a
-            v[3] = -dx * dy * dLdp;         // d/d conic.b
-            v[4] = -0.5f * dy * dy * dLdp;  // d/d conic.c
-          }
+        const float4 co = s_co[j];
+        bool contrib = unwind_step(p0, c, pxf, pyf0, m, co, s_rgbd, j, v);
+        contrib |= unwind_step(p1, c, pxf, pyf1, m, co, s_rgbd, j, v);
+        if (__ballot_sync(0xffffffffu, contrib)) {
+          float red = warp_transpose_reduce16(v, lane);
+          int k = lane >> 1;
+          if (!(lane & 1) && k < 10) s_part[warp][j][k] = red;
+        } else if (lane < 10) {
+          s_part[warp][j][lane] = 0.f;
         }
       }
-      if (__ballot_sync(0xffffffffu, contrib)) {
-        float r = warp_transpose_reduce16(v, lane);
-        int k = lane >> 1;
-        if (!(lane & 1) && k < 10) s_part[warp][j][k] = r;
-      } else if (lane < 10) {
-        s_part[warp][j][lane] = 0.f;
-      }
-     }
     }
     __syncthreads();
     if ((int)threadIdx.x < cnt) {
@@ -238,7 +262,7 @@ __global__ void __launch_bounds__(kTilePixels) k_render_bwd(RenderBwdArgs<Scenes
 
 template <class Scenes>
 void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st) {
-  k_render_bwd<Scenes><<<tiles, kTilePixels, 0, st>>>(a);
+  k_render_bwd<Scenes><<<tiles, kBwdThreads, 0, st>>>(a);
 }
 template void launch_render_bwd<SingleScene>(const RenderBwdArgs<SingleScene>&, int, cudaStream_t);
 template void launch_render_bwd<SceneTable>(const RenderBwdArgs<SceneTable>&, int, cudaStream_t);

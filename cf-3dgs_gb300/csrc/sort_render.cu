@@ -22,7 +22,8 @@ namespace cfgs {
 
 constexpr int kSortCap = 4096;   // tile segments up to this size sort in shared memory
 constexpr int kSortThreads = 256;
-constexpr int kRenderBatch = 256;
+constexpr int kRenderThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
+constexpr int kRenderBatch = 128;
 
 __device__ __forceinline__ uint32_t block_excl_scan_256(uint32_t v, uint32_t* sh, uint32_t* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -157,44 +158,57 @@ __device__ __forceinline__ int merge_split(const uint64_t* A, int la, const uint
 }
 
 // Stable LSD radix sort of a tile segment (n <= kSortCap) by the 32-bit depth bits,
-// 4 bits per pass, in shared memory: each thread owns a run of consecutive elements,
-// counts its digits into its own column of a [16][256] table, a block-wide exclusive
-// scan of the table in digit-major order gives every (digit, thread) its first output
-// slot, and the thread writes its elements in order (stable). Passes whose digit is the
-// same for all elements are skipped. Equal depths then appear in input order, which the
+// 8 bits per pass, in shared memory. Warp w owns the contiguous eighth
+// [w n/8, (w+1) n/8) of the segment and walks it 32 elements per round (conflict-free,
+// consecutive lanes on consecutive elements). Counting: per round, lanes with equal
+// digits find each other with __match_any_sync and the lowest adds their number to the
+// warp's column of a [256][8] histogram. A block-wide exclusive scan of the histogram
+// in (digit, warp) order gives each warp its first slot per digit. Scatter: per round the
+// same match gives each lane its rank among equal digits, the lowest lane advances the
+// warp's running slot. Everything before an element in the segment (earlier rounds,
+// earlier warps, lower lanes) lands before it: stable. Passes whose digit is the same
+// for all elements are skipped. Equal depths then appear in input order, which the
 // scatter left arbitrary, so each run of equal depths is re-sorted by pre-sort index:
 // the final order is (depth, pre-sort index), unique.
 struct RadixSmem {
   uint32_t key[2][kSortCap];
   uint16_t idx[2][kSortCap];
-  uint32_t cnt[16][kSortThreads + 1];
+  uint16_t hist[256][kSortThreads / 32];   // counts, then first slots
   uint32_t warp_tot[kSortThreads / 32];
-  int trivial;
 };
 
 __device__ void radix_sort_segment(RadixSmem& S, const uint64_t* keys, int n, int& out_buf) {
+  constexpr int kW = kSortThreads / 32;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const int E = (n + kSortThreads - 1) / kSortThreads;
-  const int b0 = min(n, t * E), b1 = min(n, b0 + E);
+  const int per = (n + kW - 1) / kW;
+  const int w0 = min(n, warp * per), w1 = min(n, w0 + per);
   for (int i = t; i < n; i += kSortThreads) {
     S.key[0][i] = (uint32_t)(keys[i] >> 32);
     S.idx[0][i] = (uint16_t)i;
   }
   int cur = 0;
-  for (int shift = 0; shift < 32; shift += 4) {
-#pragma unroll
-    for (int d = 0; d < 16; ++d) S.cnt[d][t] = 0;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int shift = 0; shift < 32; shift += 8) {
+    for (int d = t; d < 256 * kW; d += kSortThreads) (&S.hist[0][0])[d] = 0;
     __syncthreads();
-    for (int i = b0; i < b1; ++i) S.cnt[(S.key[cur][i] >> shift) & 15u][t]++;
+    for (int base = w0; base < w1; base += 32) {
+      const int i = base + lane;
+      const bool act = i < w1;
+      const unsigned am = __ballot_sync(0xffffffffu, act);
+      if (act) {
+        const uint32_t d = (S.key[cur][i] >> shift) & 255u;
+        const unsigned peers = __match_any_sync(am, d);
+        if ((peers & lt_mask) == 0) S.hist[d][warp] += (uint16_t)__popc(peers);
+      }
+    }
     __syncthreads();
-    // exclusive scan of cnt in digit-major order; thread t owns flat entries [16t, 16t+16)
-    uint32_t loc[16];
+    // exclusive scan in (digit, warp) order: thread t owns digit t's 8 warp entries
+    uint32_t loc[kW];
     uint32_t run = 0;
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int f = 16 * t + u;
-      loc[u] = run;
-      run += S.cnt[f >> 8][f & 255];
+    for (int w = 0; w < kW; ++w) {
+      loc[w] = run;
+      run += S.hist[t][w];
     }
     uint32_t x = run;
     for (int o = 1; o < 32; o <<= 1) {
@@ -205,28 +219,30 @@ __device__ void radix_sort_segment(RadixSmem& S, const uint64_t* keys, int n, in
     __syncthreads();
     uint32_t pre = x - run;
     for (int w = 0; w < warp; ++w) pre += S.warp_tot[w];
+    const bool trivial_local = run == (uint32_t)n;  // digit t holds every element
+    const bool trivial = __syncthreads_or(trivial_local);
+    if (trivial) continue;
 #pragma unroll
-    for (int u = 0; u < 16; ++u) {
-      const int f = 16 * t + u;
-      S.cnt[f >> 8][f & 255] = pre + loc[u];
-    }
+    for (int w = 0; w < kW; ++w) S.hist[t][w] = (uint16_t)(pre + loc[w]);
     __syncthreads();
-    bool trivial = false;  // one digit holds every element: the pass changes nothing
-#pragma unroll
-    for (int d = 0; d < 16; ++d) {
-      const uint32_t start = S.cnt[d][0], end = d < 15 ? S.cnt[d + 1][0] : (uint32_t)n;
-      trivial |= (end - start == (uint32_t)n);
-    }
-    if (trivial) {  // uniform: every thread read the same bucket starts
-      __syncthreads();
-      continue;
-    }
     const int nxt = cur ^ 1;
-    for (int i = b0; i < b1; ++i) {
-      const uint32_t k = S.key[cur][i];
-      const uint32_t pos = S.cnt[(k >> shift) & 15u][t]++;
-      S.key[nxt][pos] = k;
-      S.idx[nxt][pos] = S.idx[cur][i];
+    for (int base = w0; base < w1; base += 32) {
+      const int i = base + lane;
+      const bool act = i < w1;
+      const unsigned am = __ballot_sync(0xffffffffu, act);
+      if (act) {
+        const uint32_t k = S.key[cur][i];
+        const uint32_t d = (k >> shift) & 255u;
+        const unsigned peers = __match_any_sync(am, d);
+        const int leader = __ffs(peers) - 1;
+        const uint32_t slot0 = S.hist[d][warp];
+        const uint32_t pos = slot0 + __popc(peers & lt_mask);
+        S.key[nxt][pos] = k;
+        S.idx[nxt][pos] = S.idx[cur][i];
+        __syncwarp(am);
+        if (lane == leader) S.hist[d][warp] = (uint16_t)(slot0 + __popc(peers));
+        __syncwarp(am);
+      }
     }
     __syncthreads();
     cur = nxt;
@@ -319,18 +335,48 @@ __global__ void __launch_bounds__(kSortThreads) k_tile_sort(SortArgs a) {
   }
 }
 
-// One block per 16x16 tile, one thread per pixel; warp w covers the 8x4 pixel box
-// (8 (w & 1), 4 (w >> 1)) of the tile. Batches of 256 instances are gathered into shared
-// memory (per-Gaussian data stays L2-resident). Two exact shortcuts skip work whose
-// outcome is known: each warp keeps only the instances whose alpha >= 1/255 ellipse can
-// reach its box (box_may_contribute, one test per instance and warp), and a pixel skips
-// the exponential when the exponent lies below the instance's alpha_threshold. Neither
-// changes a decision of the published algorithm, so every output — contributor counts
-// included, which count positions in the tile's list — is what the plain loop gives.
-// Compositing runs front to back; a warp stops when its pixels are saturated and the
-// block when all are.
+// Front-to-back state of one pixel and one compositing step (the published loop body,
+// with the exponential skipped below the alpha threshold — exact, see alpha_threshold).
+struct PixelFwd {
+  float T, C0, C1, C2, D;
+  uint32_t last;
+  bool done;
+};
+
+__device__ __forceinline__ void composite_step(PixelFwd& p, float pxf, float pyf, const float4& xyt, const float4& co,
+                                               const float4* s_rgbd, int j, uint32_t pos1) {
+  if (p.done) return;
+  const float power = gauss_power(co.x, co.y, co.z, xyt.x - pxf, xyt.y - pyf);
+  if (power > 0.0f || power < xyt.z) return;
+  const float alpha = fminf(CFGS_ALPHA_MAX, co.w * exp_ref_inrange(power));
+  if (alpha < CFGS_ALPHA_MIN) return;
+  const float test_T = p.T * (1.0f - alpha);
+  if (test_T < CFGS_T_MIN) {
+    p.done = true;
+    return;
+  }
+  const float4 c = s_rgbd[j];
+  const float w = alpha * p.T;
+  p.C0 = fmaf(c.x, w, p.C0);
+  p.C1 = fmaf(c.y, w, p.C1);
+  p.C2 = fmaf(c.z, w, p.C2);
+  p.D = fmaf(c.w, w, p.D);
+  p.T = test_T;
+  p.last = pos1;
+}
+
+// One block of 128 threads per 16x16 tile; warp w covers the 8x8 pixel box
+// (8 (w & 1), 8 (w >> 1)) and each lane two pixels of it, rows r and r + 4. Batches of
+// 128 instances are gathered into shared memory (per-Gaussian data stays L2-resident).
+// Two exact shortcuts skip work whose outcome is known: each warp keeps only the
+// instances whose alpha >= 1/255 ellipse can reach its box (box_may_contribute, one test
+// per instance and warp), and a pixel skips the exponential when the exponent lies
+// below the instance's alpha_threshold. Neither changes a decision of the published
+// algorithm, so every output — contributor counts included, which count positions in
+// the tile's list — is what the plain per-pixel loop gives. Compositing runs front to
+// back; a warp stops when its pixels are saturated and the block when all are.
 template <class Scenes>
-__global__ void __launch_bounds__(kTilePixels) k_render_fwd(RenderArgs<Scenes> a) {
+__global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes> a) {
   __shared__ float4 s_xyt[kRenderBatch];   // (x, y, alpha threshold, -)
   __shared__ float4 s_co[kRenderBatch];    // (ca, cb, cc, opacity)
   __shared__ float4 s_rgbd[kRenderBatch];
@@ -340,18 +386,17 @@ __global__ void __launch_bounds__(kTilePixels) k_render_fwd(RenderArgs<Scenes> a
   const int lt = tile - sd.tile_base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int bx0 = (lt % sd.grid_x) * kTileX + (warp & 1) * 8;
-  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 4;
-  const int px = bx0 + (lane & 7), py = by0 + (lane >> 3);
-  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 3);
-  const bool inside = px < sd.W && py < sd.H;
-  const float pxf = (float)px, pyf = (float)py;
+  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 8;
+  const int px = bx0 + (lane & 7), py0 = by0 + (lane >> 3), py1 = py0 + 4;
+  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 7);
+  const bool in0 = px < sd.W && py0 < sd.H, in1 = px < sd.W && py1 < sd.H;
+  const float pxf = (float)px, pyf0 = (float)py0, pyf1 = (float)py1;
   const uint32_t lo = a.tile_range[tile];
   const int n = (int)(a.tile_range[tile + 1] - lo);
-  bool done = !inside;
-  float T = 1.0f, C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, D = 0.0f;
-  uint32_t last = 0;
+  PixelFwd p0{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0u, !in0};
+  PixelFwd p1{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0u, !in1};
   for (int base = 0; base < n; base += kRenderBatch) {
-    if (__syncthreads_count(done) == kRenderBatch) break;
+    if (__syncthreads_count(p0.done && p1.done) == kRenderThreads) break;
     int i = base + threadIdx.x;
     if (i < n) {
       uint32_t g = a.sorted_gid[lo + i];
@@ -377,46 +422,35 @@ __global__ void __launch_bounds__(kTilePixels) k_render_fwd(RenderArgs<Scenes> a
     }
 #pragma unroll
     for (int r = 0; r < kRenderBatch / 32; ++r) {
-      if (__all_sync(0xffffffffu, done)) break;
+      if (__all_sync(0xffffffffu, p0.done && p1.done)) break;
       uint32_t mk = keep[r];
       while (mk) {
         const int j = r * 32 + __ffs(mk) - 1;
         mk &= mk - 1;
-        if (done) continue;
         const float4 xyt = s_xyt[j];
         const float4 co = s_co[j];
-        const float power = gauss_power(co.x, co.y, co.z, xyt.x - pxf, xyt.y - pyf);
-        if (power > 0.0f || power < xyt.z) continue;
-        const float alpha = fminf(CFGS_ALPHA_MAX, co.w * exp_ref_inrange(power));
-        if (alpha < CFGS_ALPHA_MIN) continue;
-        const float test_T = T * (1.0f - alpha);
-        if (test_T < CFGS_T_MIN) {
-          done = true;
-          continue;
-        }
-        const float4 c = s_rgbd[j];
-        const float w = alpha * T;
-        C0 = fmaf(c.x, w, C0);
-        C1 = fmaf(c.y, w, C1);
-        C2 = fmaf(c.z, w, C2);
-        D = fmaf(c.w, w, D);
-        T = test_T;
-        last = (uint32_t)(base + j + 1);
+        const uint32_t pos1 = (uint32_t)(base + j + 1);
+        composite_step(p0, pxf, pyf0, xyt, co, s_rgbd, j, pos1);
+        composite_step(p1, pxf, pyf1, xyt, co, s_rgbd, j, pos1);
       }
     }
   }
-  if (inside) {
-    const size_t HW = (size_t)sd.W * sd.H;
+  const size_t HW = (size_t)sd.W * sd.H;
+  float* col = a.out_color + 3 * (size_t)sd.pix_base;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const PixelFwd& p = q ? p1 : p0;
+    const int py = q ? py1 : py0;
+    if (!(q ? in1 : in0)) continue;
     const size_t pix = (size_t)py * sd.W + px;
     const size_t gp = (size_t)sd.pix_base + pix;
-    a.final_T[gp] = T;
-    a.n_contrib[gp] = last;
-    float* col = a.out_color + 3 * (size_t)sd.pix_base;
-    col[pix] = fmaf(T, __ldg(sd.bg + 0), C0);
-    col[HW + pix] = fmaf(T, __ldg(sd.bg + 1), C1);
-    col[2 * HW + pix] = fmaf(T, __ldg(sd.bg + 2), C2);
-    if (a.out_depth) a.out_depth[gp] = D;
-    if (a.out_alpha) a.out_alpha[gp] = 1.0f - T;
+    a.final_T[gp] = p.T;
+    a.n_contrib[gp] = p.last;
+    col[pix] = fmaf(p.T, __ldg(sd.bg + 0), p.C0);
+    col[HW + pix] = fmaf(p.T, __ldg(sd.bg + 1), p.C1);
+    col[2 * HW + pix] = fmaf(p.T, __ldg(sd.bg + 2), p.C2);
+    if (a.out_depth) a.out_depth[gp] = p.D;
+    if (a.out_alpha) a.out_alpha[gp] = 1.0f - p.T;
   }
 }
 
@@ -437,7 +471,7 @@ void launch_tile_sort(const SortArgs& a, int tiles, cudaStream_t st) {
 }
 template <class Scenes>
 void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st) {
-  k_render_fwd<Scenes><<<tiles, kTilePixels, 0, st>>>(a);
+  k_render_fwd<Scenes><<<tiles, kRenderThreads, 0, st>>>(a);
 }
 template void launch_scatter<SingleScene>(const ScatterArgs<SingleScene>&, int, cudaStream_t);
 template void launch_scatter<SceneTable>(const ScatterArgs<SceneTable>&, int, cudaStream_t);
