@@ -29,7 +29,6 @@ for _p in (ROOT, os.path.join(ROOT, "cf-3dgs_gb300")):
 
 METRIC = "fwd+bwd iters/s at 1M Gaussians 1080p"
 UNIT = "iters/s"
-KERNELS_PER_STEP = 7  # preprocess, scan, scatter, tile sort, composite, render bwd, preprocess bwd
 
 
 def _args():
@@ -245,7 +244,7 @@ def run_ours(a) -> None:
                        "l2": "inputs larger than L2 (Gaussian parameters "
                              f"{sc.n * (44 + 12 * D) / 1e6:.0f} MB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
             "roofline": roofline, "phases": phases, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": KERNELS_PER_STEP * a.steps,
+            "gpu_launches": raster.kernel_launches(sc.camera.width, sc.camera.height)["total"] * a.steps,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -165,25 +165,25 @@ def check(status: int, what: str) -> None:
         raise RuntimeError(f"{what} failed: {STATUS.get(status, status)}")
 
 
-GEOM_FIELDS = ["xy", "conic_op", "rgbd", "rect", "touched", "offset", "clamped", "block_sums", "block_prefix",
-               "total"]
-IMAGE_FIELDS = ["counts", "tile_count", "tile_range", "tile_cursor", "final_T", "n_contrib", "total"]
-BINNING_FIELDS = ["keys", "keys_alt", "inst_gid", "sorted_gid", "sorted_pidx", "total"]
+GEOM_FIELDS = ["xy", "conic_op", "rgbd", "rect", "touched", "offset", "clamped", "block_sums", "depth_key",
+               "depth_val", "rank_sums", "depth_counts", "depth_totals", "total"]
+IMAGE_FIELDS = ["counts", "tile_count", "tile_range", "final_T", "n_contrib", "total"]
+BINNING_FIELDS = ["key", "gid", "pidx", "sorted_gid", "sorted_pidx", "chunk_counts", "totals", "total"]
 
 
 def geom_layout(n: int) -> dict:
-    arr = (C.c_size_t * 10)()
+    arr = (C.c_size_t * len(GEOM_FIELDS))()
     load().cfgs_geom_layout(int(n), arr)
     return dict(zip(GEOM_FIELDS, list(arr)))
 
 
 def image_layout(w: int, h: int) -> dict:
-    arr = (C.c_size_t * 7)()
+    arr = (C.c_size_t * len(IMAGE_FIELDS))()
     load().cfgs_image_layout(int(w), int(h), arr)
     return dict(zip(IMAGE_FIELDS, list(arr)))
 
 
 def binning_layout(cap: int) -> dict:
-    arr = (C.c_size_t * 6)()
+    arr = (C.c_size_t * len(BINNING_FIELDS))()
     load().cfgs_binning_layout(int(cap), arr)
     return dict(zip(BINNING_FIELDS, list(arr)))

@@ -262,6 +262,22 @@ def mark_visible(positions: torch.Tensor, viewmatrix: torch.Tensor, projmatrix: 
     return vis.bool()
 
 
+def kernel_launches(width: int, height: int) -> dict:
+    """Kernels the forward and backward launch for one image (N > 0): preprocess and
+    the K sum; binning = depth sort (4 radix passes of count/scan/scatter), rank sums,
+    emission, tile sort (count/scan/scatter per pass of at most 8 tile-index bits) and
+    tile ranges; compositing; render backward; preprocess backward."""
+    tiles = ((width + 15) // 16) * ((height + 15) // 16)
+    bits = 1
+    while bits < 31 and (1 << bits) < tiles:
+        bits += 1
+    tile_passes = (bits + 7) // 8
+    out = {"preprocess": 2, "bin": 4 * 3 + 2 + 3 * tile_passes + 1, "composite": 1, "render_bwd": 1,
+           "preprocess_bwd": 1}
+    out["total"] = sum(out.values())
+    return out
+
+
 def inspect_state(state: ForwardState, width: int, height: int) -> dict:
     """Typed views of the forward workspaces (for tests and debugging)."""
     import torch as _t

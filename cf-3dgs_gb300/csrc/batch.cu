@@ -94,7 +94,6 @@ BatchViews views(const CfgsBatchArgs* a) {
   v.iv.counts = reinterpret_cast<CfgsCounts*>(b + IL.header);
   v.iv.tile_count = reinterpret_cast<uint32_t*>(b + IL.tile_count);
   v.iv.tile_range = reinterpret_cast<uint32_t*>(b + IL.tile_range);
-  v.iv.tile_cursor = reinterpret_cast<uint32_t*>(b + IL.tile_cursor);
   v.iv.final_T = reinterpret_cast<float*>(b + IL.final_T);
   // n_contrib follows final_T's batch-sized array
   v.iv.n_contrib = reinterpret_cast<uint32_t*>(b + IL.n_contrib);
@@ -143,26 +142,24 @@ extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   pa.scenes = v.table;
   pa.g = g;
   pa.geom = v.gv;
-  pa.tile_count = v.iv.tile_count;
   pa.counts = v.iv.counts;
   pa.radii = a->radii;
   pa.total_slots = a->gauss_slots;
   launch_preprocess(pa, a->num_blocks, st);
-  launch_scan(v.iv.tile_count, v.iv.tile_range, v.iv.tile_cursor, a->num_tiles, v.gv.block_sums, v.gv.block_prefix,
-              a->num_blocks, v.iv.counts, st);
+  launch_scan(v.gv.block_sums, a->num_blocks, v.iv.counts, st);
 
-  ScatterArgs<SceneTable> sa;
-  sa.scenes = v.table;
-  sa.total_slots = a->gauss_slots;
-  sa.geom = v.gv;
-  sa.tile_range = v.iv.tile_range;
-  sa.tile_cursor = v.iv.tile_cursor;
-  sa.bin = v.bv;
-  sa.cap = a->capacity;
-  sa.counts = v.iv.counts;
-  launch_scatter(sa, a->num_blocks, st);
-  SortArgs so{v.iv.tile_range, v.bv, a->capacity, v.iv.counts};
-  launch_tile_sort(so, a->num_tiles, st);
+  BinArgs<SceneTable> ba;
+  ba.scenes = v.table;
+  ba.total_slots = a->gauss_slots;
+  ba.geom = v.gv;
+  ba.bin = v.bv;
+  ba.cap = a->capacity;
+  ba.counts = v.iv.counts;
+  ba.num_tiles = a->num_tiles;
+  ba.tile_count = v.iv.tile_count;
+  ba.tile_range = v.iv.tile_range;
+  int status = launch_binning(ba, st);
+  if (status != CFGS_OK) return status;
 
   RenderArgs<SceneTable> ra;
   ra.scenes = v.table;

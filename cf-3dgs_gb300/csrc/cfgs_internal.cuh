@@ -20,11 +20,22 @@ constexpr int kMaxShCoeffs = 16;  // SH degree 3
 // ---------------------------------------------------------------------------
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Depth sort of the Gaussians (binning, first stage): stable LSD radix sort of the
+// 32-bit depth keys in chunks of kSortChunk elements, kDepthPasses passes of 8 bits.
+constexpr int kSortChunk = 4096;
+constexpr int kSortDigits = 256;  // digits per pass at most (8 bits)
+constexpr int kDepthPasses = 4;
+constexpr int kMaxTilePasses = 4;
+
+__host__ __device__ inline int64_t sort_chunks(int64_t n) { return n > 0 ? (n + kSortChunk - 1) / kSortChunk : 1; }
+
 struct GeomLayout {
-  size_t xy, conic_op, rgbd, rect, touched, offset, clamped, block_sums, block_prefix, total;
+  size_t xy, conic_op, rgbd, rect, touched, offset, clamped, block_sums, depth_key, depth_val, rank_sums,
+      depth_counts, depth_totals, total;
   int32_t num_blocks;
   __host__ __device__ explicit GeomLayout(int32_t n) {
     num_blocks = (n + kPreprocessBlock - 1) / kPreprocessBlock;
+    const size_t sn = (size_t)(n > 0 ? n : 1);
     size_t o = 0;
     xy = o;           o = align256(o + sizeof(float) * 2 * (size_t)n);
     conic_op = o;     o = align256(o + sizeof(float) * 4 * (size_t)n);
@@ -34,7 +45,11 @@ struct GeomLayout {
     offset = o;       o = align256(o + sizeof(uint32_t) * (size_t)n);
     clamped = o;      o = align256(o + (size_t)n);
     block_sums = o;   o = align256(o + sizeof(uint32_t) * (size_t)(num_blocks + 1));
-    block_prefix = o; o = align256(o + sizeof(uint32_t) * (size_t)(num_blocks + 1));
+    depth_key = o;    o = align256(o + sizeof(uint32_t) * 2 * sn);
+    depth_val = o;    o = align256(o + sizeof(uint32_t) * 2 * sn);
+    rank_sums = o;    o = align256(o + sizeof(uint32_t) * (size_t)(num_blocks + 1));
+    depth_counts = o; o = align256(o + sizeof(uint32_t) * kSortDigits * (size_t)sort_chunks(n));
+    depth_totals = o; o = align256(o + sizeof(uint32_t) * kSortDigits * kDepthPasses);
     total = o;
   }
 };
@@ -45,13 +60,18 @@ struct GeomView {
   float4* rgbd;        // (r, g, b, view depth)
   uint2* rect;         // (min_x | min_y << 16, max_x | max_y << 16) in tiles
   uint32_t* touched;   // tiles touched (0 = culled)
-  uint32_t* offset;    // exclusive prefix of touched = first pre-sort instance index
+  uint32_t* offset;    // first instance index of the Gaussian (instances are numbered in depth order)
   uint8_t* clamped;    // bit c set: SH colour channel c was clamped at 0
   uint32_t* block_sums;
-  uint32_t* block_prefix;
+  uint32_t* depth_key[2];  // depth sort ping-pong keys
+  uint32_t* depth_val[2];  // depth sort ping-pong Gaussian ids; depth_val[1] = Gaussians in depth order
+  uint32_t* rank_sums;     // instances per 256 depth-ordered Gaussians
+  uint32_t* depth_counts;  // [256][chunks] per-pass digit counts, then first slots
+  uint32_t* depth_totals;  // [passes][256] digit totals
   __host__ __device__ GeomView() {}
   __host__ __device__ GeomView(void* base, int32_t n) {
     GeomLayout L(n);
+    const size_t sn = (size_t)(n > 0 ? n : 1);
     char* b = static_cast<char*>(base);
     xy = reinterpret_cast<float2*>(b + L.xy);
     conic_op = reinterpret_cast<float4*>(b + L.conic_op);
@@ -61,12 +81,18 @@ struct GeomView {
     offset = reinterpret_cast<uint32_t*>(b + L.offset);
     clamped = reinterpret_cast<uint8_t*>(b + L.clamped);
     block_sums = reinterpret_cast<uint32_t*>(b + L.block_sums);
-    block_prefix = reinterpret_cast<uint32_t*>(b + L.block_prefix);
+    depth_key[0] = reinterpret_cast<uint32_t*>(b + L.depth_key);
+    depth_key[1] = depth_key[0] + sn;
+    depth_val[0] = reinterpret_cast<uint32_t*>(b + L.depth_val);
+    depth_val[1] = depth_val[0] + sn;
+    rank_sums = reinterpret_cast<uint32_t*>(b + L.rank_sums);
+    depth_counts = reinterpret_cast<uint32_t*>(b + L.depth_counts);
+    depth_totals = reinterpret_cast<uint32_t*>(b + L.depth_totals);
   }
 };
 
 struct ImageLayout {
-  size_t header, tile_count, tile_range, tile_cursor, final_T, n_contrib, total;
+  size_t header, tile_count, tile_range, final_T, n_contrib, total;
   int32_t grid_x, grid_y, num_tiles;
   __host__ __device__ ImageLayout(int32_t w, int32_t h) {
     grid_x = (w + kTileX - 1) / kTileX;
@@ -77,7 +103,6 @@ struct ImageLayout {
     header = o;      o = align256(o + sizeof(CfgsCounts));
     tile_count = o;  o = align256(o + sizeof(uint32_t) * (size_t)num_tiles);
     tile_range = o;  o = align256(o + sizeof(uint32_t) * (size_t)(num_tiles + 1));
-    tile_cursor = o; o = align256(o + sizeof(uint32_t) * (size_t)num_tiles);
     final_T = o;     o = align256(o + sizeof(float) * px);
     n_contrib = o;   o = align256(o + sizeof(uint32_t) * px);
     total = o;
@@ -88,7 +113,6 @@ struct ImageView {
   CfgsCounts* counts;
   uint32_t* tile_count;
   uint32_t* tile_range;   // [num_tiles + 1]: tile t owns sorted positions [r[t], r[t+1])
-  uint32_t* tile_cursor;
   float* final_T;
   uint32_t* n_contrib;
   __host__ __device__ ImageView() {}
@@ -98,41 +122,54 @@ struct ImageView {
     counts = reinterpret_cast<CfgsCounts*>(b + L.header);
     tile_count = reinterpret_cast<uint32_t*>(b + L.tile_count);
     tile_range = reinterpret_cast<uint32_t*>(b + L.tile_range);
-    tile_cursor = reinterpret_cast<uint32_t*>(b + L.tile_cursor);
     final_T = reinterpret_cast<float*>(b + L.final_T);
     n_contrib = reinterpret_cast<uint32_t*>(b + L.n_contrib);
   }
 };
 
+// Instances (one per Gaussian and touched tile). The emission writes them in depth
+// order (tile key, Gaussian id; the instance index is the position); the tile sort
+// passes ping-pong between the two buffers and the last one writes sorted_gid and
+// sorted_pidx.
 struct BinningLayout {
-  size_t keys, keys_alt, inst_gid, sorted_gid, sorted_pidx, total;
+  size_t key, gid, pidx, sorted_gid, sorted_pidx, chunk_counts, totals, total;
   __host__ __device__ explicit BinningLayout(int64_t cap) {
     size_t c = cap > 0 ? (size_t)cap : 1;
     size_t o = 0;
-    keys = o;        o = align256(o + sizeof(uint64_t) * c);
-    keys_alt = o;    o = align256(o + sizeof(uint64_t) * c);
-    inst_gid = o;    o = align256(o + sizeof(uint32_t) * c);
-    sorted_gid = o;  o = align256(o + sizeof(uint32_t) * c);
-    sorted_pidx = o; o = align256(o + sizeof(uint32_t) * c);
+    key = o;          o = align256(o + sizeof(uint32_t) * 2 * c);
+    gid = o;          o = align256(o + sizeof(uint32_t) * 2 * c);
+    pidx = o;         o = align256(o + sizeof(uint32_t) * 2 * c);
+    sorted_gid = o;   o = align256(o + sizeof(uint32_t) * c);
+    sorted_pidx = o;  o = align256(o + sizeof(uint32_t) * c);
+    chunk_counts = o; o = align256(o + sizeof(uint32_t) * kSortDigits * (size_t)sort_chunks(cap));
+    totals = o;       o = align256(o + sizeof(uint32_t) * kSortDigits * kMaxTilePasses);
     total = o;
   }
 };
 
 struct BinningView {
-  uint64_t* keys;        // (depth bits << 32 | pre-sort instance index), bucketed by tile
-  uint64_t* keys_alt;    // ping-pong buffer of the large-tile merge
-  uint32_t* inst_gid;    // pre-sort instance index -> Gaussian id
-  uint32_t* sorted_gid;  // sorted position -> Gaussian id
-  uint32_t* sorted_pidx; // sorted position -> pre-sort instance index
+  uint32_t* key[2];       // global tile index of the instance
+  uint32_t* gid[2];       // Gaussian id
+  uint32_t* pidx[2];      // instance index (position in depth order)
+  uint32_t* sorted_gid;   // sorted position -> Gaussian id
+  uint32_t* sorted_pidx;  // sorted position -> instance index
+  uint32_t* chunk_counts; // [256][chunks] per-pass digit counts, then first slots
+  uint32_t* totals;       // [passes][256] digit totals
   __host__ __device__ BinningView() {}
   __host__ __device__ BinningView(void* base, int64_t cap) {
     BinningLayout L(cap);
+    const size_t c = cap > 0 ? (size_t)cap : 1;
     char* b = static_cast<char*>(base);
-    keys = reinterpret_cast<uint64_t*>(b + L.keys);
-    keys_alt = reinterpret_cast<uint64_t*>(b + L.keys_alt);
-    inst_gid = reinterpret_cast<uint32_t*>(b + L.inst_gid);
+    key[0] = reinterpret_cast<uint32_t*>(b + L.key);
+    key[1] = key[0] + c;
+    gid[0] = reinterpret_cast<uint32_t*>(b + L.gid);
+    gid[1] = gid[0] + c;
+    pidx[0] = reinterpret_cast<uint32_t*>(b + L.pidx);
+    pidx[1] = pidx[0] + c;
     sorted_gid = reinterpret_cast<uint32_t*>(b + L.sorted_gid);
     sorted_pidx = reinterpret_cast<uint32_t*>(b + L.sorted_pidx);
+    chunk_counts = reinterpret_cast<uint32_t*>(b + L.chunk_counts);
+    totals = reinterpret_cast<uint32_t*>(b + L.totals);
   }
 };
 
@@ -173,6 +210,7 @@ struct SingleScene {
   SceneDesc d;
   __device__ __forceinline__ const SceneDesc& for_block(int) const { return d; }
   __device__ __forceinline__ const SceneDesc& for_tile(int) const { return d; }
+  __device__ __forceinline__ const SceneDesc& for_gaussian(int64_t) const { return d; }
 };
 
 struct SceneTable {
@@ -181,6 +219,9 @@ struct SceneTable {
   const int32_t* tile_scene;   // global tile -> scene
   __device__ __forceinline__ const SceneDesc& for_block(int b) const { return d[block_scene[b]]; }
   __device__ __forceinline__ const SceneDesc& for_tile(int t) const { return d[tile_scene[t]]; }
+  __device__ __forceinline__ const SceneDesc& for_gaussian(int64_t g) const {
+    return d[block_scene[g / kPreprocessBlock]];
+  }
 };
 
 // Position of Gaussian i as the projection sees it: the stored mean, or R p + t in

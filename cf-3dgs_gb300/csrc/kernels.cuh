@@ -12,29 +12,35 @@ struct PreArgs {
   Scenes scenes;
   CfgsGaussians g;  // pointers index the global (padded) Gaussian arrays
   GeomView geom;
-  uint32_t* tile_count;
   CfgsCounts* counts;
   int32_t* radii;
   int64_t total_slots;  // Gaussian slots covered by the launch (padded in batches)
 };
 
+// Binning: depth sort, emission in depth order, tile sort, tile ranges.
 template <class Scenes>
-struct ScatterArgs {
+struct BinArgs {
   Scenes scenes;
   int64_t total_slots;
   GeomView geom;
-  const uint32_t* tile_range;
-  uint32_t* tile_cursor;
   BinningView bin;
   int64_t cap;
   CfgsCounts* counts;
+  int64_t num_tiles;  // all scenes' tiles
+  uint32_t* tile_count;
+  uint32_t* tile_range;
 };
 
-struct SortArgs {
-  const uint32_t* tile_range;
+template <class Scenes>
+struct EmitArgs {
+  Scenes scenes;
+  int64_t total_slots;
+  const uint32_t* order;      // Gaussians in (depth, id) order
+  const uint32_t* rank_sums;  // instances per 256 of them
+  GeomView geom;
   BinningView bin;
   int64_t cap;
-  const CfgsCounts* counts;
+  CfgsCounts* counts;
 };
 
 template <class Scenes>
@@ -95,11 +101,9 @@ struct PreBwdArgs {
 
 template <class Scenes>
 void launch_preprocess(const PreArgs<Scenes>& a, int blocks, cudaStream_t st);
-void launch_scan(uint32_t* tile_count, uint32_t* tile_range, uint32_t* tile_cursor, int num_tiles,
-                 uint32_t* block_sums, uint32_t* block_prefix, int num_blocks, CfgsCounts* counts, cudaStream_t st);
+void launch_scan(uint32_t* block_sums, int num_blocks, CfgsCounts* counts, cudaStream_t st);
 template <class Scenes>
-void launch_scatter(const ScatterArgs<Scenes>& a, int blocks, cudaStream_t st);
-void launch_tile_sort(const SortArgs& a, int tiles, cudaStream_t st);
+int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st);
 template <class Scenes>
 void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st);
 template <class Scenes>

@@ -277,9 +277,6 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs<Scenes>
           a.geom.clamped[idx] = cl;
           touched = area;
           radius = rad;
-          uint32_t* counts = a.tile_count + sd.tile_base;
-          for (int ty = rminy; ty < rmaxy; ++ty)
-            for (int tx = rminx; tx < rmaxx; ++tx) atomicAdd(&counts[ty * sd.grid_x + tx], 1u);
         }
       }
     }
@@ -300,54 +297,20 @@ void launch_preprocess(const PreArgs<Scenes>& a, int blocks, cudaStream_t st) {
 template void launch_preprocess<SingleScene>(const PreArgs<SingleScene>&, int, cudaStream_t);
 template void launch_preprocess<SceneTable>(const PreArgs<SceneTable>&, int, cudaStream_t);
 
-// Exclusive scan of `n` uint32 values by one block of 1024 threads; returns the total.
-__device__ uint64_t block_exclusive_scan(const uint32_t* in, uint32_t* out, int n, uint32_t* sh) {
-  uint64_t carry = 0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int base = 0; base < n; base += blockDim.x) {
-    int i = base + threadIdx.x;
-    uint32_t v = i < n ? in[i] : 0u;
-    uint32_t x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) sh[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t w = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0u;
-      for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-        if (lane >= o) w += y;
-      }
-      sh[32 + lane] = w;  // inclusive warp totals
-    }
-    __syncthreads();
-    uint32_t warp_prefix = warp > 0 ? sh[32 + warp - 1] : 0u;
-    uint64_t excl = carry + warp_prefix + (x - v);
-    if (i < n) out[i] = (uint32_t)excl;
-    uint32_t chunk_total = sh[32 + (blockDim.x >> 5) - 1];
-    __syncthreads();
-    carry += chunk_total;
-  }
-  return carry;
-}
-
-// One block: tile counts -> tile ranges (K), block sums -> block prefixes.
-__global__ void __launch_bounds__(1024) k_scan(uint32_t* tile_count, uint32_t* tile_range,
-                                               uint32_t* tile_cursor, int num_tiles,
-                                               uint32_t* block_sums, uint32_t* block_prefix,
-                                               int num_blocks, CfgsCounts* counts) {
-  __shared__ uint32_t sh[64];
-  uint64_t K = block_exclusive_scan(tile_count, tile_range, num_tiles, sh);
-  for (int i = threadIdx.x; i < num_tiles; i += blockDim.x) tile_cursor[i] = 0u;
+// Instance count K = sum of the per-block touched sums (one block of 1024 threads).
+__global__ void __launch_bounds__(1024) k_scan(const uint32_t* block_sums, int num_blocks, CfgsCounts* counts) {
+  __shared__ unsigned long long sh[32];
+  unsigned long long v = 0;
+  for (int i = threadIdx.x; i < num_blocks; i += blockDim.x) v += block_sums[i];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    uint32_t k32 = K > 0xffffffffull ? 0xffffffffu : (uint32_t)K;
-    tile_range[num_tiles] = k32;
-    counts->num_rendered = k32;
+    unsigned long long K = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) K += sh[w];
+    counts->num_rendered = K > 0xffffffffull ? 0xffffffffu : (uint32_t)K;
     if (K > 0x7fffffffull) atomicOr(&counts->flags, CFGS_FLAG_CAPACITY_OVERFLOW);
   }
-  block_exclusive_scan(block_sums, block_prefix, num_blocks, sh);
 }
 
 __global__ void __launch_bounds__(256) k_mark_visible(int n, const float* means, const float* V,
@@ -362,10 +325,8 @@ __global__ void __launch_bounds__(256) k_mark_visible(int n, const float* means,
   vis[i] = t.z <= CFGS_NEAR_Z ? 0 : 1;
 }
 
-void launch_scan(uint32_t* tile_count, uint32_t* tile_range, uint32_t* tile_cursor, int num_tiles,
-                 uint32_t* block_sums, uint32_t* block_prefix, int num_blocks, CfgsCounts* counts, cudaStream_t st) {
-  k_scan<<<1, 1024, 0, st>>>(tile_count, tile_range, tile_cursor, num_tiles, block_sums, block_prefix, num_blocks,
-                             counts);
+void launch_scan(uint32_t* block_sums, int num_blocks, CfgsCounts* counts, cudaStream_t st) {
+  k_scan<<<1, 1024, 0, st>>>(block_sums, num_blocks, counts);
 }
 
 }  // namespace cfgs
@@ -381,20 +342,16 @@ extern "C" size_t cfgs_backward_scratch_bytes(int64_t cap) {
   return align256(sizeof(float) * 4 * kRecordFloat4 * (size_t)(cap > 0 ? cap : 1));
 }
 
-extern "C" void cfgs_geom_layout(int32_t n, size_t o[10]) {
+extern "C" void cfgs_geom_layout(int32_t n, size_t o[14]) {
   GeomLayout L(n < 0 ? 0 : n);
-  size_t v[10] = {L.xy, L.conic_op, L.rgbd, L.rect, L.touched, L.offset, L.clamped, L.block_sums, L.block_prefix,
-                  L.total};
-  for (int i = 0; i < 10; ++i) o[i] = v[i];
+  size_t v[14] = {L.xy,        L.conic_op,  L.rgbd,         L.rect,         L.touched,
+                  L.offset,    L.clamped,   L.block_sums,   L.depth_key,    L.depth_val,
+                  L.rank_sums, L.depth_counts, L.depth_totals, L.total};
+  for (int i = 0; i < 14; ++i) o[i] = v[i];
 }
-extern "C" void cfgs_image_layout(int32_t w, int32_t h, size_t o[7]) {
+extern "C" void cfgs_image_layout(int32_t w, int32_t h, size_t o[6]) {
   ImageLayout L(w < 1 ? 1 : w, h < 1 ? 1 : h);
-  size_t v[7] = {L.header, L.tile_count, L.tile_range, L.tile_cursor, L.final_T, L.n_contrib, L.total};
-  for (int i = 0; i < 7; ++i) o[i] = v[i];
-}
-extern "C" void cfgs_binning_layout(int64_t cap, size_t o[6]) {
-  BinningLayout L(cap);
-  size_t v[6] = {L.keys, L.keys_alt, L.inst_gid, L.sorted_gid, L.sorted_pidx, L.total};
+  size_t v[6] = {L.header, L.tile_count, L.tile_range, L.final_T, L.n_contrib, L.total};
   for (int i = 0; i < 6; ++i) o[i] = v[i];
 }
 
@@ -429,15 +386,13 @@ extern "C" int cfgs_preprocess_forward(const CfgsSettings* s, const CfgsGaussian
     a.scenes.d = single_scene_desc(s, g->num_gaussians, g->sh_coeffs);
     a.g = *g;
     a.geom = gv;
-    a.tile_count = iv.tile_count;
     a.counts = iv.counts;
     a.radii = radii;
     a.total_slots = g->num_gaussians;
     k_preprocess<SingleScene><<<GL.num_blocks, kPreprocessBlock, 0, st>>>(a);
     CFGS_CHECK_LAUNCH(s->debug, st);
   }
-  k_scan<<<1, 1024, 0, st>>>(iv.tile_count, iv.tile_range, iv.tile_cursor, IL.num_tiles,
-                             gv.block_sums, gv.block_prefix, GL.num_blocks, iv.counts);
+  k_scan<<<1, 1024, 0, st>>>(gv.block_sums, GL.num_blocks, iv.counts);
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;
 }

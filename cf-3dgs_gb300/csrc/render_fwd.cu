@@ -1,0 +1,184 @@
+// Forward phase 3: front-to-back alpha compositing of every 16x16 tile over its
+// depth-sorted instance list.
+//
+// The kernel is a template over the scene accessor (one scene for the drop-in path, a
+// descriptor table for batched solves); the arithmetic is the same for both.
+// Compiled with -fmad=false; the fmaf() calls are the only fused operations, and the
+// CPU oracle performs the same sequence.
+#include "cfgs_internal.cuh"
+#include "kernels.cuh"
+
+namespace cfgs {
+
+constexpr int kRenderThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
+constexpr int kRenderBatch = 128;
+
+// Front-to-back state of one pixel and one compositing step (the published loop body,
+// with the exponential skipped below the alpha threshold — exact, see alpha_threshold).
+struct PixelFwd {
+  float T, C0, C1, C2, D;
+  uint32_t last;
+  bool done;
+};
+
+__device__ __forceinline__ void composite_step(PixelFwd& p, float pxf, float pyf, const float4& xyt, const float4& co,
+                                               const float4* s_rgbd, int j, uint32_t pos1) {
+  if (p.done) return;
+  const float power = gauss_power(co.x, co.y, co.z, xyt.x - pxf, xyt.y - pyf);
+  if (power > 0.0f || power < xyt.z) return;
+  const float alpha = fminf(CFGS_ALPHA_MAX, co.w * exp_ref_inrange(power));
+  if (alpha < CFGS_ALPHA_MIN) return;
+  const float test_T = p.T * (1.0f - alpha);
+  if (test_T < CFGS_T_MIN) {
+    p.done = true;
+    return;
+  }
+  const float4 c = s_rgbd[j];
+  const float w = alpha * p.T;
+  p.C0 = fmaf(c.x, w, p.C0);
+  p.C1 = fmaf(c.y, w, p.C1);
+  p.C2 = fmaf(c.z, w, p.C2);
+  p.D = fmaf(c.w, w, p.D);
+  p.T = test_T;
+  p.last = pos1;
+}
+
+// One block of 128 threads per 16x16 tile; warp w covers the 8x8 pixel box
+// (8 (w & 1), 8 (w >> 1)) and each lane two pixels of it, rows r and r + 4. Batches of
+// 128 instances are gathered into shared memory (per-Gaussian data stays L2-resident).
+// Two exact shortcuts skip work whose outcome is known: each warp keeps only the
+// instances whose alpha >= 1/255 ellipse can reach its box (box_may_contribute, one test
+// per instance and warp), and a pixel skips the exponential when the exponent lies
+// below the instance's alpha_threshold. Neither changes a decision of the published
+// algorithm, so every output — contributor counts included, which count positions in
+// the tile's list — is what the plain per-pixel loop gives. Compositing runs front to
+// back; a warp stops when its pixels are saturated and the block when all are.
+template <class Scenes>
+__global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes> a) {
+  __shared__ float4 s_xyt[kRenderBatch];   // (x, y, alpha threshold, -)
+  __shared__ float4 s_co[kRenderBatch];    // (ca, cb, cc, opacity)
+  __shared__ float4 s_rgbd[kRenderBatch];
+  if ((int64_t)a.counts->num_rendered > a.cap) return;
+  const int tile = blockIdx.x;
+  const SceneDesc& sd = a.scenes.for_tile(tile);
+  const int lt = tile - sd.tile_base;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bx0 = (lt % sd.grid_x) * kTileX + (warp & 1) * 8;
+  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 8;
+  const int px = bx0 + (lane & 7), py0 = by0 + (lane >> 3), py1 = py0 + 4;
+  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 7);
+  const bool in0 = px < sd.W && py0 < sd.H, in1 = px < sd.W && py1 < sd.H;
+  const float pxf = (float)px, pyf0 = (float)py0, pyf1 = (float)py1;
+  const uint32_t lo = a.tile_range[tile];
+  const int n = (int)(a.tile_range[tile + 1] - lo);
+  PixelFwd p0{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0u, !in0};
+  PixelFwd p1{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0u, !in1};
+  for (int base = 0; base < n; base += kRenderBatch) {
+    if (__syncthreads_count(p0.done && p1.done) == kRenderThreads) break;
+    int i = base + threadIdx.x;
+    if (i < n) {
+      uint32_t g = a.sorted_gid[lo + i];
+      float2 m = a.xy[g];
+      float4 co = a.conic_op[g];
+      s_xyt[threadIdx.x] = make_float4(m.x, m.y, alpha_threshold(co.w), 0.0f);
+      s_co[threadIdx.x] = make_float4(-0.5f * co.x, -co.y, -0.5f * co.z, co.w);
+      s_rgbd[threadIdx.x] = a.rgbd[g];
+    }
+    __syncthreads();
+    const int cnt = min(kRenderBatch, n - base);
+    uint32_t keep[kRenderBatch / 32];
+#pragma unroll
+    for (int r = 0; r < kRenderBatch / 32; ++r) {
+      const int j = r * 32 + lane;
+      bool k = false;
+      if (j < cnt) {
+        const float4 xyt = s_xyt[j];
+        const float4 co = s_co[j];
+        k = box_may_contribute(make_float2(xyt.x, xyt.y), co.x, co.y, co.z, xyt.z, bxf0, bxf1, byf0, byf1);
+      }
+      keep[r] = __ballot_sync(0xffffffffu, k);
+    }
+#pragma unroll
+    for (int r = 0; r < kRenderBatch / 32; ++r) {
+      if (__all_sync(0xffffffffu, p0.done && p1.done)) break;
+      uint32_t mk = keep[r];
+      while (mk) {
+        const int j = r * 32 + __ffs(mk) - 1;
+        mk &= mk - 1;
+        const float4 xyt = s_xyt[j];
+        const float4 co = s_co[j];
+        const uint32_t pos1 = (uint32_t)(base + j + 1);
+        composite_step(p0, pxf, pyf0, xyt, co, s_rgbd, j, pos1);
+        composite_step(p1, pxf, pyf1, xyt, co, s_rgbd, j, pos1);
+      }
+    }
+  }
+  const size_t HW = (size_t)sd.W * sd.H;
+  float* col = a.out_color + 3 * (size_t)sd.pix_base;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const PixelFwd& p = q ? p1 : p0;
+    const int py = q ? py1 : py0;
+    if (!(q ? in1 : in0)) continue;
+    const size_t pix = (size_t)py * sd.W + px;
+    const size_t gp = (size_t)sd.pix_base + pix;
+    a.final_T[gp] = p.T;
+    a.n_contrib[gp] = p.last;
+    col[pix] = fmaf(p.T, __ldg(sd.bg + 0), p.C0);
+    col[HW + pix] = fmaf(p.T, __ldg(sd.bg + 1), p.C1);
+    col[2 * HW + pix] = fmaf(p.T, __ldg(sd.bg + 2), p.C2);
+    if (a.out_depth) a.out_depth[gp] = p.D;
+    if (a.out_alpha) a.out_alpha[gp] = 1.0f - p.T;
+  }
+}
+
+template <class Scenes>
+void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st) {
+  k_render_fwd<Scenes><<<tiles, kRenderThreads, 0, st>>>(a);
+}
+template void launch_render_fwd<SingleScene>(const RenderArgs<SingleScene>&, int, cudaStream_t);
+template void launch_render_fwd<SceneTable>(const RenderArgs<SceneTable>&, int, cudaStream_t);
+
+}  // namespace cfgs
+
+using namespace cfgs;
+
+extern "C" int cfgs_composite_forward(const CfgsSettings* s, int32_t num_gaussians, const void* geom, const void* image,
+                                      const void* binning, int64_t capacity, float* out_color, float* out_depth,
+                                      float* out_alpha, void* stream) {
+  if (!s || !geom || !image || !binning || !out_color || capacity < 0 || !s->bg || num_gaussians < 0)
+    return CFGS_ERR_INVALID_ARGUMENT;
+  if (s->image_width <= 0 || s->image_height <= 0) return CFGS_ERR_INVALID_ARGUMENT;
+  if (capacity > 0x7fffffffll) return CFGS_ERR_TOO_LARGE;
+  cudaStream_t st = (cudaStream_t)stream;
+  ImageLayout IL(s->image_width, s->image_height);
+  ImageView iv(const_cast<void*>(image), s->image_width, s->image_height);
+  GeomView gv(const_cast<void*>(geom), num_gaussians);
+  BinningView bv(const_cast<void*>(binning), capacity);
+  RenderArgs<SingleScene> ra;
+  ra.scenes.d = single_scene_desc(s, num_gaussians, 0);
+  ra.tile_range = iv.tile_range;
+  ra.sorted_gid = bv.sorted_gid;
+  ra.xy = gv.xy;
+  ra.conic_op = gv.conic_op;
+  ra.rgbd = gv.rgbd;
+  ra.final_T = iv.final_T;
+  ra.n_contrib = iv.n_contrib;
+  ra.out_color = out_color;
+  ra.out_depth = out_depth;
+  ra.out_alpha = out_alpha;
+  ra.cap = capacity;
+  ra.counts = iv.counts;
+  launch_render_fwd(ra, IL.num_tiles, st);
+  CFGS_CHECK_LAUNCH(s->debug, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_render_forward(const CfgsSettings* s, const CfgsGaussians* g, void* geom, void* image,
+                                   void* binning, int64_t capacity, float* out_color, float* out_depth,
+                                   float* out_alpha, void* stream) {
+  int st = cfgs_bin_forward(s, g, geom, image, binning, capacity, stream);
+  if (st != CFGS_OK) return st;
+  return cfgs_composite_forward(s, g->num_gaussians, geom, image, binning, capacity, out_color, out_depth, out_alpha,
+                                stream);
+}

@@ -116,21 +116,24 @@ size_t cfgs_backward_scratch_bytes(int64_t capacity);
 
 /* Byte offsets of the arrays inside the workspaces, for inspection (tests, debugging;
  * upstream exposes the same buffers as opaque uint8 tensors).
- * geom  (10): xy float2, conic_op float4 (a,b,c,opacity), rgbd float4 (r,g,b,depth),
- *             rect uint2 (x0|y0<<16, x1|y1<<16), touched u32, offset u32, clamped u8,
- *             block_sums u32, block_prefix u32, total bytes
- * image (7):  counts CfgsCounts, tile_count u32, tile_range u32[T+1], tile_cursor u32,
- *             final_T f32, n_contrib u32, total bytes
- * binning (6): keys u64, keys_alt u64, inst_gid u32, sorted_gid u32, sorted_pidx u32,
- *             total bytes */
-void cfgs_geom_layout(int32_t num_gaussians, size_t offsets[10]);
-void cfgs_image_layout(int32_t image_width, int32_t image_height, size_t offsets[7]);
-void cfgs_binning_layout(int64_t capacity, size_t offsets[6]);
+ * geom  (14): xy float2, conic_op float4 (a,b,c,opacity), rgbd float4 (r,g,b,depth),
+ *             rect uint2 (x0|y0<<16, x1|y1<<16), touched u32, offset u32 (first instance
+ *             index), clamped u8, block_sums u32, depth_key u32[2][N], depth_val u32[2][N]
+ *             (depth_val[1] = Gaussian ids in (depth, id) order), rank_sums u32,
+ *             depth_counts u32, depth_totals u32, total bytes
+ * image (6):  counts CfgsCounts, tile_count u32, tile_range u32[T+1], final_T f32,
+ *             n_contrib u32, total bytes
+ * binning (8): key u32[2][cap] (tile), gid u32[2][cap], pidx u32[2][cap],
+ *             sorted_gid u32, sorted_pidx u32 (instance index), chunk_counts u32,
+ *             totals u32, total bytes */
+void cfgs_geom_layout(int32_t num_gaussians, size_t offsets[14]);
+void cfgs_image_layout(int32_t image_width, int32_t image_height, size_t offsets[6]);
+void cfgs_binning_layout(int64_t capacity, size_t offsets[8]);
 
 /* ---- rasteriser forward, phase 1 ---------------------------------------------
  * Replaces the first half of upstream rasterize_gaussians (markVisible/preprocess
  * /InclusiveSum): projects every Gaussian (EWA), evaluates SH colour, computes the
- * screen radius and tile rectangle, counts instances per tile and scans them.
+ * screen radius and tile rectangle, and sums the tiles touched.
  * Writes radii[N] (0 = culled) and K into the image workspace. */
 int cfgs_preprocess_forward(const CfgsSettings* settings, const CfgsGaussians* gaussians,
                             void* geom, void* image, int32_t* radii, void* stream);
@@ -140,10 +143,10 @@ int cfgs_preprocess_forward(const CfgsSettings* settings, const CfgsGaussians* g
 int cfgs_read_counts(const void* image, CfgsCounts* counts_host, void* stream);
 
 /* ---- rasteriser forward, phase 2 ---------------------------------------------
- * Replaces duplicateWithKeys / SortPairs / identifyTileRanges / render: emits the
- * K (tile, depth) instances, sorts them per tile by (view depth, instance index) —
- * the order a stable sort of upstream's 64-bit key (tile << 32 | depth bits) gives —
- * and alpha-composites every 16x16 tile front to back.
+ * Replaces duplicateWithKeys / SortPairs / identifyTileRanges / render: sorts the
+ * Gaussians by (view depth, id), emits the K (tile, Gaussian) instances in that order,
+ * sorts them stably by tile — the order a stable sort of upstream's 64-bit key
+ * (tile << 32 | depth bits) gives — and alpha-composites every 16x16 tile front to back.
  * out_color [3,H,W], out_depth [1,H,W], out_alpha [1,H,W]. `capacity` is the number
  * of instances the binning workspace holds; the device K is used, and if it exceeds
  * `capacity` the kernels raise CFGS_FLAG_CAPACITY_OVERFLOW and write nothing past it. */
@@ -152,8 +155,9 @@ int cfgs_render_forward(const CfgsSettings* settings, const CfgsGaussians* gauss
                         float* out_color, float* out_depth, float* out_alpha, void* stream);
 
 /* The two halves of cfgs_render_forward, for callers that time or schedule them
- * separately: instance emission + per-tile sort (duplicateWithKeys / SortPairs /
- * identifyTileRanges upstream), then compositing (renderCUDA upstream). */
+ * separately: depth sort + instance emission + tile sort + tile ranges
+ * (duplicateWithKeys / SortPairs / identifyTileRanges upstream), then compositing
+ * (renderCUDA upstream). */
 int cfgs_bin_forward(const CfgsSettings* settings, const CfgsGaussians* gaussians, void* geom, void* image,
                      void* binning, int64_t capacity, void* stream);
 int cfgs_composite_forward(const CfgsSettings* settings, int32_t num_gaussians, const void* geom,
@@ -245,8 +249,8 @@ int cfgs_pose_adam(int32_t count, float* xi, const float* grad, float* state, do
 /* ---- batched pose solves ----------------------------------------------------------
  * Many CF-3DGS pose solves (trainer/cf3dgs_trainer.py:261-285), each with its own
  * Gaussians, camera and resolution, advance together: one call runs one Adam iteration
- * of every solve with one launch per stage (preprocess, scan, scatter, tile sort,
- * composite, render backward with the RGB L1 image gradient formed in-kernel, pose-only
+ * of every solve with one launch per stage (preprocess, scan, depth sort, emission,
+ * tile sort, tile ranges, composite, render backward with the RGB L1 image gradient formed in-kernel, pose-only
  * preprocess backward, per-solve pose update). Nothing synchronises, so a sequence of
  * iterations can be captured in a CUDA graph. Per solve the arithmetic is that of the
  * single-solve path (cfgs_pose_apply -> rasteriser -> cfgs_pose_grad -> cfgs_pose_adam).

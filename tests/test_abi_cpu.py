@@ -40,7 +40,7 @@ def test_workspace_sizes_and_layouts():
     assert im["n_contrib"] - im["final_T"] >= 1920 * 1080 * 4
     b = native.binning_layout(12345)
     assert b["total"] == lib.cfgs_binning_bytes(12345)
-    assert b["keys_alt"] - b["keys"] >= 12345 * 8
+    assert b["gid"] - b["key"] >= 12345 * 8 and b["sorted_pidx"] - b["sorted_gid"] >= 12345 * 4
     assert lib.cfgs_backward_scratch_bytes(1000) >= 1000 * 48
     assert lib.cfgs_image_bytes(0, 10) == 0
 
