@@ -21,7 +21,7 @@
 // scatter (rank inside the chunk, stage in shared memory by digit, then write each
 // digit's run to its global slots). Ranking inside a chunk is stable: warp w owns the
 // contiguous slice [w C/8, (w+1) C/8) and walks it 32 elements per round; lanes with
-// equal digits find each other with __match_any_sync.
+// equal digits find each other with one ballot per digit bit.
 #include "cfgs_internal.cuh"
 #include "kernels.cuh"
 
@@ -29,13 +29,12 @@ namespace cfgs {
 
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = kSortChunk / kSortThreads;  // 16 elements per thread
-constexpr int kWarpSlice = kSortChunk / kSortWarps;     // 512 elements per warp
+constexpr int kMaxDigitBits = 8;
 
-// One radix pass. Keys come from key_in, or (depth mode, key_in == NULL) from the
-// geometry: the depth bits of Gaussians that touch a tile, ~0 for the others, so they
-// sort last. Payloads come from val_in / aux_in, or are the element's own index when
-// those are NULL.
+// One radix pass over elements [0, n) split into chunks of `chunk` elements. Keys come
+// from key_in, or (depth mode) from the geometry: the depth bits of Gaussians that
+// touch a tile, ~0 for the others, so they sort last. Payloads come from val_in /
+// aux_in, or are the element's own index when those are NULL.
 struct SortPass {
   const uint32_t* key_in;
   const uint32_t* val_in;
@@ -55,38 +54,80 @@ struct SortPass {
   uint32_t* digit_totals;      // [1 << bits], zero before the count launch
 };
 
-__device__ __forceinline__ int64_t pass_elements(const SortPass& p) {
-  if (!p.counts) return p.n;
+__device__ __forceinline__ uint32_t pass_elements(const SortPass& p) {
+  if (!p.counts) return (uint32_t)p.n;
   const int64_t k = (int64_t)p.counts->num_rendered;
-  return k > p.cap ? 0 : k;
+  return k > p.cap ? 0u : (uint32_t)k;
 }
 
-__device__ __forceinline__ uint32_t pass_key(const SortPass& p, int64_t i) {
-  if (p.key_in) return p.key_in[i];
-  return p.depth_touched[i] ? __float_as_uint(p.depth_rgbd[i].w) : 0xffffffffu;
+// Loads the keys of elements [c0 + 4 j, c0 + 4 j + 4) (those below n) with one vector
+// load where the four are in range.
+template <bool DEPTH>
+__device__ __forceinline__ uint4 load_keys4(const SortPass& p, uint32_t i, uint32_t n) {
+  uint4 k = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+  if (DEPTH) {
+    uint32_t* kk = &k.x;
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (i + e < n) kk[e] = p.depth_touched[i + e] ? __float_as_uint(p.depth_rgbd[i + e].w) : 0xffffffffu;
+  } else if (i + 3 < n) {
+    k = *reinterpret_cast<const uint4*>(p.key_in + i);
+  } else {
+    uint32_t* kk = &k.x;
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (i + e < n) kk[e] = p.key_in[i + e];
+  }
+  return k;
 }
 
+__device__ __forceinline__ uint4 load_u32x4(const uint32_t* a, uint32_t i, uint32_t n) {
+  if (i + 3 < n) return *reinterpret_cast<const uint4*>(a + i);
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  uint32_t* vv = &v.x;
+#pragma unroll
+  for (int e = 0; e < 4; ++e)
+    if (i + e < n) vv[e] = a[i + e];
+  return v;
+}
+
+// Lanes of `active` whose digit equals this lane's: one ballot per digit bit. Every
+// lane of the warp must call it.
+__device__ __forceinline__ unsigned digit_peers(uint32_t d, int bits, unsigned active) {
+  unsigned peers = active;
+#pragma unroll
+  for (int b = 0; b < kMaxDigitBits; ++b) {
+    if (b < bits) {
+      const bool set = (d >> b) & 1u;
+      const unsigned bal = __ballot_sync(0xffffffffu, set);
+      peers &= set ? bal : ~bal;
+    }
+  }
+  return peers;
+}
+
+// Digit histogram of one chunk (per-warp shared-memory counters), written to
+// chunk_counts[d][chunk] and added to digit_totals[d].
+template <int CHUNK, bool DEPTH>
 __global__ void __launch_bounds__(kSortThreads) k_sort_count(SortPass p) {
   __shared__ uint32_t hist[kSortWarps][kSortDigits];
-  const int64_t n = pass_elements(p);
-  const int64_t c0 = (int64_t)blockIdx.x * kSortChunk;
+  const uint32_t n = pass_elements(p);
+  const uint32_t c0 = blockIdx.x * (uint32_t)CHUNK;
   if (c0 >= n) return;
-  const int cnt = (int)min((int64_t)kSortChunk, n - c0);
   const int ndig = 1 << p.bits;
   const uint32_t mask = (uint32_t)ndig - 1u;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < kSortWarps * kSortDigits; i += kSortThreads) (&hist[0][0])[i] = 0u;
   __syncthreads();
-  const unsigned lt = (1u << lane) - 1u;
-#pragma unroll 4
-  for (int k = 0; k < kSortItems; ++k) {
-    const int i = warp * kWarpSlice + k * 32 + lane;
-    const bool act = i < cnt;
-    const unsigned am = __ballot_sync(0xffffffffu, act);
-    if (act) {
-      const uint32_t d = (pass_key(p, c0 + i) >> p.shift) & mask;
-      const unsigned peers = __match_any_sync(am, d);
-      if ((peers & lt) == 0) hist[warp][d] += (uint32_t)__popc(peers);
+#pragma unroll
+  for (int k = 0; k < CHUNK / (4 * kSortThreads); ++k) {
+    const uint32_t i = c0 + 4u * (k * kSortThreads + threadIdx.x);
+    if (i < n) {
+      const uint4 kk = load_keys4<DEPTH>(p, i, n);
+      atomicAdd(&hist[warp][(kk.x >> p.shift) & mask], 1u);
+      if (i + 1 < n) atomicAdd(&hist[warp][(kk.y >> p.shift) & mask], 1u);
+      if (i + 2 < n) atomicAdd(&hist[warp][(kk.z >> p.shift) & mask], 1u);
+      if (i + 3 < n) atomicAdd(&hist[warp][(kk.w >> p.shift) & mask], 1u);
     }
   }
   __syncthreads();
@@ -130,12 +171,13 @@ __device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t v, uint32_t* s
 // One block per digit d: chunk_counts[d][c] becomes the global slot of digit d's first
 // element in chunk c = (elements with a smaller digit) + (digit-d elements of earlier
 // chunks).
+template <int CHUNK>
 __global__ void __launch_bounds__(1024) k_sort_scan(SortPass p) {
   __shared__ uint32_t sh[64];
-  const int64_t n = pass_elements(p);
-  if (n <= 0) return;
+  const uint32_t n = pass_elements(p);
+  if (n == 0) return;
   const int d = blockIdx.x;
-  const int64_t nc = (n + kSortChunk - 1) / kSortChunk;
+  const int64_t nc = ((int64_t)n + CHUNK - 1) / CHUNK;
   uint32_t tot;
   const uint32_t below = (int)threadIdx.x < d ? p.digit_totals[threadIdx.x] : 0u;
   block_inclusive_scan(below, sh, &tot);
@@ -150,53 +192,74 @@ __global__ void __launch_bounds__(1024) k_sort_scan(SortPass p) {
   }
 }
 
-// Dynamic shared memory of the scatter: staged keys and payloads, per-warp digit
-// counters, per-digit block-local starts and global slots.
-inline size_t scatter_smem(bool aux) {
-  return sizeof(uint32_t) * ((aux ? 3 : 2) * (size_t)kSortChunk + (size_t)kSortWarps * kSortDigits + 2 * kSortDigits);
-}
+// Shared memory of the scatter: keys and payloads in input order, the permutation
+// (sorted position -> input position), per-warp digit counters, per-digit block-local
+// starts and global slots.
+template <int CHUNK>
+struct ScatterSmem {
+  static constexpr size_t kKey = 0;
+  static constexpr size_t kVal = kKey + 4 * CHUNK;
+  static constexpr size_t kAux = kVal + 4 * CHUNK;
+  __host__ __device__ static size_t perm(bool aux) { return kAux + (aux ? 4 * CHUNK : 0); }
+  __host__ __device__ static size_t whist(bool aux) { return perm(aux) + 2 * CHUNK; }
+  __host__ __device__ static size_t start(bool aux) { return whist(aux) + 4 * kSortWarps * kSortDigits; }
+  __host__ __device__ static size_t slot(bool aux) { return start(aux) + 4 * kSortDigits; }
+  __host__ __device__ static size_t bytes(bool aux) { return slot(aux) + 4 * kSortDigits; }
+};
 
-__global__ void __launch_bounds__(kSortThreads, 2) k_sort_scatter(SortPass p) {
-  extern __shared__ __align__(16) uint32_t smem[];
-  const bool has_aux = p.aux_out != nullptr;
-  uint32_t* s_key = smem;
-  uint32_t* s_val = s_key + kSortChunk;
-  uint32_t* s_aux = s_val + kSortChunk;
-  uint32_t* s_whist = s_val + (has_aux ? 2 : 1) * kSortChunk;  // [warp][digit]
-  uint32_t* s_start = s_whist + kSortWarps * kSortDigits;       // block-local first position of a digit
-  uint32_t* s_slot = s_start + kSortDigits;                      // global first slot of a digit
+template <int CHUNK, bool DEPTH>
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(SortPass p) {
+  using L = ScatterSmem<CHUNK>;
+  constexpr int kSlice = CHUNK / kSortWarps;  // elements per warp
+  constexpr int kRounds = kSlice / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const bool has_val = p.val_in != nullptr, has_aux = p.aux_in != nullptr;
+  uint32_t* s_key = reinterpret_cast<uint32_t*>(smem_raw + L::kKey);
+  uint32_t* s_val = reinterpret_cast<uint32_t*>(smem_raw + L::kVal);
+  uint32_t* s_aux = reinterpret_cast<uint32_t*>(smem_raw + L::kAux);
+  uint16_t* s_perm = reinterpret_cast<uint16_t*>(smem_raw + L::perm(has_aux));
+  uint32_t* s_whist = reinterpret_cast<uint32_t*>(smem_raw + L::whist(has_aux));  // [warp][digit]
+  uint32_t* s_start = reinterpret_cast<uint32_t*>(smem_raw + L::start(has_aux));
+  uint32_t* s_slot = reinterpret_cast<uint32_t*>(smem_raw + L::slot(has_aux));
   __shared__ uint32_t sh[64];
 
-  const int64_t n = pass_elements(p);
-  const int64_t c0 = (int64_t)blockIdx.x * kSortChunk;
+  const uint32_t n = pass_elements(p);
+  const uint32_t c0 = blockIdx.x * (uint32_t)CHUNK;
   if (c0 >= n) return;
-  const int cnt = (int)min((int64_t)kSortChunk, n - c0);
+  const int cnt = (int)min((uint32_t)CHUNK, n - c0);
   const int ndig = 1 << p.bits;
   const uint32_t mask = (uint32_t)ndig - 1u;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+
+  // input chunk -> shared memory (vector loads, all in flight together)
+#pragma unroll
+  for (int k = 0; k < CHUNK / (4 * kSortThreads); ++k) {
+    const int j = 4 * (k * kSortThreads + t);
+    const uint32_t i = c0 + (uint32_t)j;
+    if (i < n) {
+      *reinterpret_cast<uint4*>(s_key + j) = load_keys4<DEPTH>(p, i, n);
+      if (has_val) *reinterpret_cast<uint4*>(s_val + j) = load_u32x4(p.val_in, i, n);
+      if (has_aux) *reinterpret_cast<uint4*>(s_aux + j) = load_u32x4(p.aux_in, i, n);
+    }
+  }
   for (int i = t; i < kSortWarps * kSortDigits; i += kSortThreads) s_whist[i] = 0u;
   __syncthreads();
 
   // rank of every element among the equal digits of its warp's slice
-  uint32_t key[kSortItems], rank[kSortItems];
+  uint32_t rank[kRounds];
   const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
-    const int i = warp * kWarpSlice + k * 32 + lane;
+  for (int k = 0; k < kRounds; ++k) {
+    const int i = warp * kSlice + k * 32 + lane;
     const bool act = i < cnt;
     const unsigned am = __ballot_sync(0xffffffffu, act);
-    key[k] = 0u;
-    rank[k] = 0u;
-    if (act) {
-      key[k] = pass_key(p, c0 + i);
-      const uint32_t d = (key[k] >> p.shift) & mask;
-      const unsigned peers = __match_any_sync(am, d);
-      const uint32_t before = s_whist[warp * kSortDigits + d];
-      rank[k] = before + (uint32_t)__popc(peers & lt);
-      __syncwarp(am);
-      if ((peers & lt) == 0) s_whist[warp * kSortDigits + d] = before + (uint32_t)__popc(peers);
-      __syncwarp(am);
-    }
+    const uint32_t d = act ? (s_key[i] >> p.shift) & mask : 0u;
+    const unsigned peers = digit_peers(d, p.bits, am);
+    const uint32_t before = act ? s_whist[warp * kSortDigits + d] : 0u;
+    rank[k] = before + (uint32_t)__popc(peers & lt);
+    __syncwarp();
+    if (act && (peers & lt) == 0) s_whist[warp * kSortDigits + d] = before + (uint32_t)__popc(peers);
+    __syncwarp();
   }
   __syncthreads();
 
@@ -218,34 +281,31 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_sort_scatter(SortPass p) {
   }
   __syncthreads();
 
-  // stage in block-local sorted order
+  // permutation: block-local sorted position -> input position
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
-    const int i = warp * kWarpSlice + k * 32 + lane;
+  for (int k = 0; k < kRounds; ++k) {
+    const int i = warp * kSlice + k * 32 + lane;
     if (i < cnt) {
-      const uint32_t d = (key[k] >> p.shift) & mask;
-      const uint32_t pos = s_start[d] + s_whist[warp * kSortDigits + d] + rank[k];
-      const int64_t gi = c0 + i;
-      s_key[pos] = key[k];
-      s_val[pos] = p.val_in ? p.val_in[gi] : (uint32_t)gi;
-      if (has_aux) s_aux[pos] = p.aux_in ? p.aux_in[gi] : (uint32_t)gi;
+      const uint32_t d = (s_key[i] >> p.shift) & mask;
+      s_perm[s_start[d] + s_whist[warp * kSortDigits + d] + rank[k]] = (uint16_t)i;
     }
   }
   __syncthreads();
 
   // each digit's run goes to consecutive global slots
   for (int q = t; q < cnt; q += kSortThreads) {
-    const uint32_t kk = s_key[q];
+    const int o = s_perm[q];
+    const uint32_t kk = s_key[o];
     const uint32_t d = (kk >> p.shift) & mask;
-    const size_t g = (size_t)s_slot[d] + (uint32_t)q - s_start[d];
+    const uint32_t g = s_slot[d] + (uint32_t)q - s_start[d];
     if (p.key_out) p.key_out[g] = kk;
-    p.val_out[g] = s_val[q];
-    if (has_aux) p.aux_out[g] = s_aux[q];
+    p.val_out[g] = has_val ? s_val[o] : c0 + (uint32_t)o;
+    if (p.aux_out) p.aux_out[g] = has_aux ? s_aux[o] : c0 + (uint32_t)o;
     if (p.tile_count) {
       // The chunk is fully sorted now (its input was sorted by the lower digits), so
       // equal tiles form runs: a run [b, e) adds e - b.
-      if (q == 0 || s_key[q - 1] != kk) atomicSub(&p.tile_count[kk], (uint32_t)q);
-      if (q == cnt - 1 || s_key[q + 1] != kk) atomicAdd(&p.tile_count[kk], (uint32_t)(q + 1));
+      if (q == 0 || s_key[s_perm[q - 1]] != kk) atomicSub(&p.tile_count[kk], (uint32_t)q);
+      if (q == cnt - 1 || s_key[s_perm[q + 1]] != kk) atomicAdd(&p.tile_count[kk], (uint32_t)(q + 1));
     }
   }
 }
@@ -264,38 +324,45 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_rank_sums(const uint32_t* 
 // One thread per depth-ordered Gaussian; the block's first instance index is the sum
 // of the earlier blocks' rank_sums, the thread's is that plus a block scan. The
 // instances are then written warp-cooperatively: the warp's instances are dealt out
-// 32 per round, one per lane, so the stores of a round are consecutive.
+// 32 per round, one per lane, so the stores of a round are consecutive. In a round, the
+// lanes whose instance ranges meet it mark where their range begins (an OR reduction),
+// and a lane's owner is the last mark at or before it; the owner's rectangle comes over
+// by shuffle. Instance j of a rectangle of width w is tile row j / w, column j % w; the
+// quotient is estimated with a float reciprocal (off by at most one for j < 2^22) and
+// corrected exactly.
 template <class Scenes>
 __global__ void __launch_bounds__(kPreprocessBlock) k_emit(EmitArgs<Scenes> a) {
   __shared__ uint32_t sh[64];
-  __shared__ uint32_t s_start[kPreprocessBlock];
-  __shared__ uint32_t s_first[kPreprocessBlock];
-  __shared__ uint32_t s_gid[kPreprocessBlock];
-  __shared__ uint2 s_rect[kPreprocessBlock];
-  __shared__ uint2 s_scene[kPreprocessBlock];  // (tile_base, grid_x)
+  __shared__ uint8_t s_owner[kPreprocessBlock / 32][32];
   if ((int64_t)a.counts->num_rendered > a.cap) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.counts->flags, CFGS_FLAG_CAPACITY_OVERFLOW);
     return;
   }
   uint32_t pre = 0, tot;
+#pragma unroll 4
   for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) pre += a.rank_sums[b];
   block_inclusive_scan(pre, sh, &tot);
   const uint32_t block_first = tot;
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31, wbase = threadIdx.x & ~31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t g = 0, nt = 0;
   if (r < a.total_slots) {
     g = a.order[r];
     nt = a.geom.touched[g];
   }
   const uint32_t first = block_first + block_inclusive_scan(nt, sh, &tot) - nt;
+  uint2 rc = make_uint2(0u, 0u);
+  uint32_t tile_base = 0, grid_x = 0;
+  float rinv = 0.0f;
   if (nt) {
     a.geom.offset[g] = first;
     const SceneDesc& sd = a.scenes.for_gaussian(g);
-    s_rect[threadIdx.x] = a.geom.rect[g];
-    s_scene[threadIdx.x] = make_uint2((uint32_t)sd.tile_base, (uint32_t)sd.grid_x);
+    rc = a.geom.rect[g];
+    tile_base = (uint32_t)sd.tile_base;
+    grid_x = (uint32_t)sd.grid_x;
+    rinv = 1.0f / (float)((rc.y & 0xffffu) - (rc.x & 0xffffu));
   }
-  // warp-inclusive scan of nt -> each lane's first warp-local instance
+  // warp-exclusive start of this lane's instances
   uint32_t x = nt;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -303,30 +370,48 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_emit(EmitArgs<Scenes> a) {
     if (lane >= o) x += y;
   }
   const uint32_t warp_total = __shfl_sync(0xffffffffu, x, 31);
-  s_start[threadIdx.x] = x - nt;
-  s_first[threadIdx.x] = first;
-  s_gid[threadIdx.x] = g;
-  __syncwarp();
+  const uint32_t start = x - nt;
+  const unsigned upto = 0xffffffffu >> (31 - lane);  // bits 0..lane
   for (uint32_t base = 0; base < warp_total; base += 32) {
-    const uint32_t w = base + lane;
-    if (w >= warp_total) break;
-    // owner lane: the last lane whose start <= w (lanes with nt == 0 share starts)
-    int lo = 0, hi = 31;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (s_start[wbase + mid] <= w) lo = mid;
-      else hi = mid - 1;
+    const bool meets = nt != 0 && start < base + 32u && start + nt > base;
+    const uint32_t pos = start > base ? start - base : 0u;
+    const unsigned marks = __reduce_or_sync(0xffffffffu, meets ? (1u << pos) : 0u);
+    if (meets) s_owner[warp][pos] = (uint8_t)lane;
+    __syncwarp();
+    const int o = s_owner[warp][31 - __clz(marks & upto)];
+    __syncwarp();
+    const uint32_t o_start = __shfl_sync(0xffffffffu, start, o);
+    const uint32_t o_rx = __shfl_sync(0xffffffffu, rc.x, o);
+    const uint32_t o_ry = __shfl_sync(0xffffffffu, rc.y, o);
+    const uint32_t o_first = __shfl_sync(0xffffffffu, first, o);
+    const uint32_t o_gid = __shfl_sync(0xffffffffu, g, o);
+    const float o_rinv = __shfl_sync(0xffffffffu, rinv, o);
+    const uint32_t o_tb = __shfl_sync(0xffffffffu, tile_base, o);
+    const uint32_t o_gx = __shfl_sync(0xffffffffu, grid_x, o);
+    const uint32_t w = base + (uint32_t)lane;
+    if (w < warp_total) {
+      const uint32_t j = w - o_start;
+      const uint32_t x0 = o_rx & 0xffffu, y0 = o_rx >> 16;
+      const uint32_t rw = (o_ry & 0xffffu) - x0;
+      uint32_t ty, tx;
+      if (j < (1u << 22)) {
+        ty = (uint32_t)((float)j * o_rinv);
+        tx = j - ty * rw;
+        if ((int32_t)tx < 0) {
+          --ty;
+          tx += rw;
+        } else if (tx >= rw) {
+          ++ty;
+          tx -= rw;
+        }
+      } else {
+        ty = j / rw;
+        tx = j - ty * rw;
+      }
+      const uint32_t q = o_first + j;
+      a.bin.key[0][q] = o_tb + (y0 + ty) * o_gx + x0 + tx;
+      a.bin.gid[0][q] = o_gid;
     }
-    const int ol = wbase + lo;
-    const uint32_t j = w - s_start[ol];
-    const uint2 rc = s_rect[ol];
-    const uint32_t x0 = rc.x & 0xffffu, y0 = rc.x >> 16, x1 = rc.y & 0xffffu;
-    const uint32_t rw = x1 - x0;
-    const uint32_t ty = y0 + j / rw, tx = x0 + j % rw;
-    const uint2 sc = s_scene[ol];
-    const uint32_t q = s_first[ol] + j;
-    a.bin.key[0][q] = sc.x + ty * sc.y + tx;
-    a.bin.gid[0][q] = s_gid[ol];
   }
 }
 
@@ -346,19 +431,20 @@ __global__ void __launch_bounds__(1024) k_tile_ranges(const uint32_t* tile_count
 
 namespace {
 
-bool g_scatter_attr_set = false;
-
+template <int CHUNK, bool DEPTH>
 int launch_pass(const SortPass& p, cudaStream_t st) {
-  if (!g_scatter_attr_set) {
-    if (cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scatter_smem(true)) !=
-        cudaSuccess)
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(k_sort_scatter<CHUNK, DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)ScatterSmem<CHUNK>::bytes(true)) != cudaSuccess)
       return CFGS_ERR_LAUNCH;
-    g_scatter_attr_set = true;
+    attr_set = true;
   }
   const int grid = (int)p.num_chunks;
-  k_sort_count<<<grid, kSortThreads, 0, st>>>(p);
-  k_sort_scan<<<1 << p.bits, 1024, 0, st>>>(p);
-  k_sort_scatter<<<grid, kSortThreads, scatter_smem(p.aux_out != nullptr), st>>>(p);
+  k_sort_count<CHUNK, DEPTH><<<grid, kSortThreads, 0, st>>>(p);
+  k_sort_scan<CHUNK><<<1 << p.bits, 1024, 0, st>>>(p);
+  k_sort_scatter<CHUNK, DEPTH>
+      <<<grid, kSortThreads, ScatterSmem<CHUNK>::bytes(p.aux_in != nullptr), st>>>(p);
   return CFGS_OK;
 }
 
@@ -398,10 +484,10 @@ int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {
       p.bits = 8;
       p.n = slots;
       p.cap = slots;
-      p.num_chunks = sort_chunks(slots);
+      p.num_chunks = sort_chunks(slots, kDepthChunk);
       p.chunk_counts = gv.depth_counts;
       p.digit_totals = gv.depth_totals + kSortDigits * pass;
-      int s = launch_pass(p, st);
+      int s = src < 0 ? launch_pass<kDepthChunk, true>(p, st) : launch_pass<kDepthChunk, false>(p, st);
       if (s != CFGS_OK) return s;
       src = dst;
     }
@@ -440,10 +526,10 @@ int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {
     p.bits = width;
     p.counts = a.counts;
     p.cap = a.cap;
-    p.num_chunks = sort_chunks(a.cap);
+    p.num_chunks = sort_chunks(a.cap, kTileChunk);
     p.chunk_counts = bv.chunk_counts;
     p.digit_totals = bv.totals + kSortDigits * pass;
-    int s = launch_pass(p, st);
+    int s = launch_pass<kTileChunk, false>(p, st);
     if (s != CFGS_OK) return s;
     src = dst;
   }

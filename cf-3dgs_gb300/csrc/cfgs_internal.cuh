@@ -20,14 +20,19 @@ constexpr int kMaxShCoeffs = 16;  // SH degree 3
 // ---------------------------------------------------------------------------
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// Depth sort of the Gaussians (binning, first stage): stable LSD radix sort of the
-// 32-bit depth keys in chunks of kSortChunk elements, kDepthPasses passes of 8 bits.
-constexpr int kSortChunk = 4096;
+// Binning sorts (stable LSD radix, at most 8 bits per pass) work on chunks of
+// elements: kDepthChunk for the depth sort of the Gaussians (4 passes), kTileChunk for
+// the tile sort of the instances.
+constexpr int kDepthChunk = 1024;
+constexpr int kTileChunk = 2048;
 constexpr int kSortDigits = 256;  // digits per pass at most (8 bits)
 constexpr int kDepthPasses = 4;
 constexpr int kMaxTilePasses = 4;
 
-__host__ __device__ inline int64_t sort_chunks(int64_t n) { return n > 0 ? (n + kSortChunk - 1) / kSortChunk : 1; }
+__host__ __device__ inline int64_t sort_chunks(int64_t n, int chunk) { return n > 0 ? (n + chunk - 1) / chunk : 1; }
+// Element stride of the halves of a ping-pong sort buffer: a multiple of 64 elements, so
+// both halves start on a 256-byte boundary (the sort passes use 16-byte vector loads).
+__host__ __device__ inline size_t pingpong_stride(int64_t n) { return ((size_t)(n > 0 ? n : 1) + 63) & ~size_t(63); }
 
 struct GeomLayout {
   size_t xy, conic_op, rgbd, rect, touched, offset, clamped, block_sums, depth_key, depth_val, rank_sums,
@@ -35,7 +40,7 @@ struct GeomLayout {
   int32_t num_blocks;
   __host__ __device__ explicit GeomLayout(int32_t n) {
     num_blocks = (n + kPreprocessBlock - 1) / kPreprocessBlock;
-    const size_t sn = (size_t)(n > 0 ? n : 1);
+    const size_t sn = pingpong_stride(n);
     size_t o = 0;
     xy = o;           o = align256(o + sizeof(float) * 2 * (size_t)n);
     conic_op = o;     o = align256(o + sizeof(float) * 4 * (size_t)n);
@@ -48,7 +53,7 @@ struct GeomLayout {
     depth_key = o;    o = align256(o + sizeof(uint32_t) * 2 * sn);
     depth_val = o;    o = align256(o + sizeof(uint32_t) * 2 * sn);
     rank_sums = o;    o = align256(o + sizeof(uint32_t) * (size_t)(num_blocks + 1));
-    depth_counts = o; o = align256(o + sizeof(uint32_t) * kSortDigits * (size_t)sort_chunks(n));
+    depth_counts = o; o = align256(o + sizeof(uint32_t) * kSortDigits * (size_t)sort_chunks(n, kDepthChunk));
     depth_totals = o; o = align256(o + sizeof(uint32_t) * kSortDigits * kDepthPasses);
     total = o;
   }
@@ -71,7 +76,7 @@ struct GeomView {
   __host__ __device__ GeomView() {}
   __host__ __device__ GeomView(void* base, int32_t n) {
     GeomLayout L(n);
-    const size_t sn = (size_t)(n > 0 ? n : 1);
+    const size_t sn = pingpong_stride(n);
     char* b = static_cast<char*>(base);
     xy = reinterpret_cast<float2*>(b + L.xy);
     conic_op = reinterpret_cast<float4*>(b + L.conic_op);
@@ -134,14 +139,14 @@ struct ImageView {
 struct BinningLayout {
   size_t key, gid, pidx, sorted_gid, sorted_pidx, chunk_counts, totals, total;
   __host__ __device__ explicit BinningLayout(int64_t cap) {
-    size_t c = cap > 0 ? (size_t)cap : 1;
+    const size_t c = pingpong_stride(cap);
     size_t o = 0;
     key = o;          o = align256(o + sizeof(uint32_t) * 2 * c);
     gid = o;          o = align256(o + sizeof(uint32_t) * 2 * c);
     pidx = o;         o = align256(o + sizeof(uint32_t) * 2 * c);
     sorted_gid = o;   o = align256(o + sizeof(uint32_t) * c);
     sorted_pidx = o;  o = align256(o + sizeof(uint32_t) * c);
-    chunk_counts = o; o = align256(o + sizeof(uint32_t) * kSortDigits * (size_t)sort_chunks(cap));
+    chunk_counts = o; o = align256(o + sizeof(uint32_t) * kSortDigits * (size_t)sort_chunks(cap, kTileChunk));
     totals = o;       o = align256(o + sizeof(uint32_t) * kSortDigits * kMaxTilePasses);
     total = o;
   }
@@ -158,7 +163,7 @@ struct BinningView {
   __host__ __device__ BinningView() {}
   __host__ __device__ BinningView(void* base, int64_t cap) {
     BinningLayout L(cap);
-    const size_t c = cap > 0 ? (size_t)cap : 1;
+    const size_t c = pingpong_stride(cap);
     char* b = static_cast<char*>(base);
     key[0] = reinterpret_cast<uint32_t*>(b + L.key);
     key[1] = key[0] + c;
