@@ -3,47 +3,41 @@
 // direction), in a full form (all eight gradient arrays, the drop-in path) and a
 // pose-only form (dL/dmean reduced straight into SE(3) gradient terms, batched solves).
 //
-// Phase 1 sums each Gaussian's per-tile records (contiguous, in pre-sort order) one
-// warp per Gaussian: coalesced 48-byte record loads, a transposing warp reduction, the
-// sums to shared memory. Phase 2 is one thread per Gaussian. Both orders are fixed, so
-// the result is deterministic.
+// Phase 1 sums each Gaussian's per-tile records (contiguous: instance indices
+// [offset, offset + touched)) eight lanes per Gaussian, four Gaussians per warp at a
+// time: strided 48-byte record loads, a transposing reduction inside each group of
+// eight lanes, the sums to shared memory. Phase 2 is one thread per Gaussian. Both
+// orders are fixed, so the result is deterministic.
 #include "cfgs_internal.cuh"
 #include "kernels.cuh"
 
 namespace cfgs {
 
-// Sums 16 per-lane values across the warp in 16 shuffles; lane L ends with the total
-// of value index L >> 1.
-__device__ __forceinline__ float warp_sum16(float (&v)[16], int lane) {
+// Sums 16 per-lane values over each group of eight lanes (lanes 8m .. 8m+7) in 14
+// shuffles; lane 8m + s ends with the group totals of value indices 2s and 2s + 1 in
+// v[0] and v[1].
+__device__ __forceinline__ void group8_sum16(float (&v)[16], int lane) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    bool up = lane & 16;
-    float send = up ? v[k] : v[k + 8];
-    float keep = up ? v[k + 8] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    const bool up = lane & 4;
+    const float send = up ? v[k] : v[k + 8];
+    const float keep = up ? v[k + 8] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
   }
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    bool up = lane & 8;
-    float send = up ? v[k] : v[k + 4];
-    float keep = up ? v[k + 4] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    const bool up = lane & 2;
+    const float send = up ? v[k] : v[k + 4];
+    const float keep = up ? v[k + 4] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
   }
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
-    bool up = lane & 4;
-    float send = up ? v[k] : v[k + 2];
-    float keep = up ? v[k + 2] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    const bool up = lane & 1;
+    const float send = up ? v[k] : v[k + 2];
+    const float keep = up ? v[k + 2] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
   }
-  {
-    bool up = lane & 2;
-    float send = up ? v[0] : v[1];
-    float keep = up ? v[1] : v[0];
-    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
-  }
-  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-  return v[0];
 }
 
 // SH backward at unit direction (x,y,z): dL/dsh[k][c] = b_k g_c (g already masked by
@@ -126,7 +120,7 @@ __device__ __forceinline__ void sh_backward(int deg, int M, const float* sh, flo
 // block's SE(3) gradient terms — sum g and sum (R p) x g in float64 with the scene's
 // float64 rotation and the un-posed positions p — go to pose_partials[block].
 template <class Scenes>
-__global__ void __launch_bounds__(256) k_preprocess_bwd(PreBwdArgs<Scenes> a) {
+__global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a) {
   __shared__ float s_acc[256][11];
   __shared__ double s_red[8][6];
   if ((int64_t)a.counts->num_rendered > a.cap) return;  // forward overflowed: outputs untouched
@@ -135,32 +129,36 @@ __global__ void __launch_bounds__(256) k_preprocess_bwd(PreBwdArgs<Scenes> a) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t blk0 = (int64_t)blockIdx.x * blockDim.x;
 
-  // ---- phase 1: record sums, one warp per Gaussian ---------------------------------
-  for (int gi = 0; gi < 32; ++gi) {
-    const int local = warp * 32 + gi;
-    const int64_t gidx = blk0 + local;
-    uint32_t nt = 0, off = 0;
-    if (gidx < a.total_slots && gidx - sd.gauss_base < sd.num_gaussians && a.radii[gidx] > 0) {
-      nt = a.geom.touched[gidx];
-      off = a.geom.offset[gidx];
+  // ---- phase 1: record sums, eight lanes per Gaussian ------------------------------
+  {
+    const int64_t gl = blk0 + warp * 32 + lane;  // this lane's Gaussian (metadata only)
+    uint32_t nt_l = 0, off_l = 0;
+    if (gl < a.total_slots && gl - sd.gauss_base < sd.num_gaussians && a.radii[gl] > 0) {
+      nt_l = a.geom.touched[gl];
+      off_l = a.geom.offset[gl];
     }
-    if (nt == 0) {
-      if (lane < 10) s_acc[local][lane] = 0.f;
-      continue;
-    }
-    float v[16];
+    const int sub = lane & 7, grp = lane >> 3;
+#pragma unroll 1
+    for (int gi = 0; gi < 32; gi += 4) {
+      const int src = gi + grp;
+      const uint32_t nt = __shfl_sync(0xffffffffu, nt_l, src);
+      const uint32_t off = __shfl_sync(0xffffffffu, off_l, src);
+      float v[16];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) v[k] = 0.f;
-    for (uint32_t r = lane; r < nt; r += 32) {
-      const float4* rec = a.records + (size_t)kRecordFloat4 * (off + r);
-      const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
-      v[0] += r0.x; v[1] += r0.y; v[2] += r0.z; v[3] += r0.w;
-      v[4] += r1.x; v[5] += r1.y; v[6] += r1.z; v[7] += r1.w;
-      v[8] += r2.x; v[9] += r2.y;
+      for (int k = 0; k < 16; ++k) v[k] = 0.f;
+      for (uint32_t r = sub; r < nt; r += 8) {
+        const float4* rec = a.records + (size_t)kRecordFloat4 * (off + r);
+        const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
+        v[0] += r0.x; v[1] += r0.y; v[2] += r0.z; v[3] += r0.w;
+        v[4] += r1.x; v[5] += r1.y; v[6] += r1.z; v[7] += r1.w;
+        v[8] += r2.x; v[9] += r2.y;
+      }
+      group8_sum16(v, lane);
+      if (sub < 5) {
+        s_acc[warp * 32 + src][2 * sub] = v[0];
+        s_acc[warp * 32 + src][2 * sub + 1] = v[1];
+      }
     }
-    const float s = warp_sum16(v, lane);
-    const int k = lane >> 1;
-    if (!(lane & 1) && k < 10) s_acc[local][k] = s;
   }
   __syncthreads();
 
