@@ -64,7 +64,7 @@ __device__ __forceinline__ float l1_grad(float c, float t, float inv_numel) {
 // Back-to-front state of one pixel: its upstream gradients, the transmittance being
 // unwound and the running colour/depth behind the current instance.
 struct PixelBwd {
-  float T_final, dC0, dC1, dC2, dD, dA, bg_dot;
+  float T_final, dC0, dC1, dC2, dD, dA_bg;  // dA_bg = dL/dalpha - bg . dL/dcolor
   float T, acc0, acc1, acc2, accd, last_a, last0, last1, last2, lastd;
   uint32_t last;
 };
@@ -76,7 +76,8 @@ __device__ __forceinline__ void load_pixel(PixelBwd& p, const RenderBwdArgs<Scen
   const size_t HW = (size_t)sd.W * sd.H;
   const size_t gp = (size_t)sd.pix_base + pix;
   p.T_final = 1.0f;
-  p.dC0 = p.dC1 = p.dC2 = p.dD = p.dA = 0.f;
+  p.dC0 = p.dC1 = p.dC2 = p.dD = 0.f;
+  float dA = 0.f;
   p.last = 0;
   if (inside) {
     p.T_final = a.final_T[gp];
@@ -91,18 +92,22 @@ __device__ __forceinline__ void load_pixel(PixelBwd& p, const RenderBwdArgs<Scen
       p.dC1 = a.dL_dcolor[cb + HW];
       p.dC2 = a.dL_dcolor[cb + 2 * HW];
       if (a.dL_ddepth) p.dD = a.dL_ddepth[gp];
-      if (a.dL_dalpha) p.dA = a.dL_dalpha[gp];
+      if (a.dL_dalpha) dA = a.dL_dalpha[gp];
     }
   }
-  p.bg_dot = __ldg(sd.bg + 0) * p.dC0 + __ldg(sd.bg + 1) * p.dC1 + __ldg(sd.bg + 2) * p.dC2;
+  p.dA_bg = dA - (__ldg(sd.bg + 0) * p.dC0 + __ldg(sd.bg + 1) * p.dC1 + __ldg(sd.bg + 2) * p.dC2);
   p.T = p.T_final;
   p.acc0 = p.acc1 = p.acc2 = p.accd = 0.f;
   p.last_a = p.last0 = p.last1 = p.last2 = p.lastd = 0.f;
 }
 
-// Unwinds one instance at list position c for one pixel and adds its ten gradient terms
-// (d mean2D x/y, d conic a/b/c, d opacity, d rgb, d depth) to v. Returns whether the
-// instance contributed to the pixel in the forward pass.
+// Unwinds one instance at list position c for one pixel and adds its terms to v:
+// with g = G dL/dalpha (G the Gaussian's value at the pixel, d = mean - pixel),
+// v0..v4 += g (dx, dy, dx^2, dx dy, dy^2), v5 += g, v6..v8 += w dL/drgb, v9 += w
+// dL/ddepth (w = alpha T). The per-instance factors (opacity, conic) are applied after
+// the reduction (finish_record). Returns whether the instance contributed to the pixel
+// in the forward pass.
+template <bool DEPTH>
 __device__ __forceinline__ bool unwind_step(PixelBwd& p, int c, float pxf, float pyf, const float4& m,
                                             const float4& co, const float4* s_rgbd, int j, float (&v)[16]) {
   if (c >= (int)p.last) return false;
@@ -113,35 +118,54 @@ __device__ __forceinline__ bool unwind_step(PixelBwd& p, int c, float pxf, float
   const float alpha = fminf(CFGS_ALPHA_MAX, co.w * G);
   if (alpha < CFGS_ALPHA_MIN) return false;
   const float4 col = s_rgbd[j];
-  const float inv_one_m = __frcp_rn(1.0f - alpha);
+  float inv_one_m;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv_one_m) : "f"(1.0f - alpha));
   p.T = p.T * inv_one_m;
   const float w = alpha * p.T;
-  v[6] += p.dC0 * w;
-  v[7] += p.dC1 * w;
-  v[8] += p.dC2 * w;
-  v[9] += p.dD * w;
-  p.acc0 = p.last_a * p.last0 + (1.f - p.last_a) * p.acc0;
-  p.acc1 = p.last_a * p.last1 + (1.f - p.last_a) * p.acc1;
-  p.acc2 = p.last_a * p.last2 + (1.f - p.last_a) * p.acc2;
-  p.accd = p.last_a * p.lastd + (1.f - p.last_a) * p.accd;
+  v[6] = fmaf(p.dC0, w, v[6]);
+  v[7] = fmaf(p.dC1, w, v[7]);
+  v[8] = fmaf(p.dC2, w, v[8]);
+  p.acc0 = fmaf(p.last_a, p.last0 - p.acc0, p.acc0);
+  p.acc1 = fmaf(p.last_a, p.last1 - p.acc1, p.acc1);
+  p.acc2 = fmaf(p.last_a, p.last2 - p.acc2, p.acc2);
+  float dLda = (col.x - p.acc0) * p.dC0;
+  dLda = fmaf(col.y - p.acc1, p.dC1, dLda);
+  dLda = fmaf(col.z - p.acc2, p.dC2, dLda);
+  if (DEPTH) {
+    v[9] = fmaf(p.dD, w, v[9]);
+    p.accd = fmaf(p.last_a, p.lastd - p.accd, p.accd);
+    dLda = fmaf(col.w - p.accd, p.dD, dLda);
+    p.lastd = col.w;
+  }
   p.last0 = col.x;
   p.last1 = col.y;
   p.last2 = col.z;
-  p.lastd = col.w;
   p.last_a = alpha;
-  float dLda = (col.x - p.acc0) * p.dC0 + (col.y - p.acc1) * p.dC1 + (col.z - p.acc2) * p.dC2 + (col.w - p.accd) * p.dD;
   dLda *= p.T;
-  const float tf = p.T_final * inv_one_m;
-  dLda += tf * (p.dA - p.bg_dot);
-  v[5] += G * dLda;                      // d/d opacity (straight through the 0.99 clamp)
-  const float dLdp = G * (co.w * dLda);  // d/d power
-  // power = ca dx^2 + cb dx dy + cc dy^2, dx = mean.x - pixel.x
-  v[0] += dLdp * (2.f * co.x * dx + co.y * dy);
-  v[1] += dLdp * (2.f * co.z * dy + co.y * dx);
-  v[2] += -0.5f * dx * dx * dLdp;  // d/d conic.a
-  v[3] += -dx * dy * dLdp;         // d/d conic.b
-  v[4] += -0.5f * dy * dy * dLdp;  // d/d conic.c
+  dLda = fmaf(p.T_final * inv_one_m, p.dA_bg, dLda);
+  const float g = G * dLda;  // d/d opacity (straight through the 0.99 clamp)
+  v[5] += g;
+  const float gx = g * dx, gy = g * dy;
+  v[0] += gx;
+  v[1] += gy;
+  v[2] = fmaf(gx, dx, v[2]);
+  v[3] = fmaf(gx, dy, v[3]);
+  v[4] = fmaf(gy, dy, v[4]);
   return true;
+}
+
+// Record of one instance from its summed terms s (unwind_step) and its (ca, cb, cc,
+// opacity): power = ca dx^2 + cb dx dy + cc dy^2 with ca = -A/2, cb = -B, cc = -C/2 for
+// the conic (A, B, C), so dL/dpower = opacity g and
+//   dL/dmean2D = opacity (2 ca Sx + cb Sy, 2 cc Sy + cb Sx),
+//   dL/d(A, B, C) = -opacity (Sxx / 2, Sxy, Syy / 2).
+__device__ __forceinline__ void finish_record(float4* rec, const float (&s)[10], const float4& co) {
+  const float op = co.w;
+  const float dmx = op * fmaf(2.f * co.x, s[0], co.y * s[1]);
+  const float dmy = op * fmaf(2.f * co.z, s[1], co.y * s[0]);
+  rec[0] = make_float4(dmx, dmy, -0.5f * op * s[2], -op * s[3]);
+  rec[1] = make_float4(-0.5f * op * s[4], s[5], s[6], s[7]);
+  rec[2] = make_float4(s[8], s[9], 0.f, 0.f);
 }
 
 // One block of 128 threads per tile with the forward's pixel boxes (warp w: 8x8 box,
@@ -149,7 +173,7 @@ __device__ __forceinline__ bool unwind_step(PixelBwd& p, int c, float pxf, float
 // instance, alpha_threshold per pixel). A lane adds its two pixels' terms before the
 // warp reduction; the cross-warp sum of an instance adds only the warps that kept it
 // (the others' terms are exact zeros).
-template <class Scenes>
+template <class Scenes, bool DEPTH>
 __global__ void __launch_bounds__(kBwdThreads) k_render_bwd(RenderBwdArgs<Scenes> a) {
   __shared__ float4 s_xyt[kBwdBatch];
   __shared__ float4 s_co[kBwdBatch];
@@ -224,8 +248,8 @@ __global__ void __launch_bounds__(kBwdThreads) k_render_bwd(RenderBwdArgs<Scenes
         for (int k = 0; k < 16; ++k) v[k] = 0.f;
         const float4 m = s_xyt[j];
         const float4 co = s_co[j];
-        bool contrib = unwind_step(p0, c, pxf, pyf0, m, co, s_rgbd, j, v);
-        contrib |= unwind_step(p1, c, pxf, pyf1, m, co, s_rgbd, j, v);
+        bool contrib = unwind_step<DEPTH>(p0, c, pxf, pyf0, m, co, s_rgbd, j, v);
+        contrib |= unwind_step<DEPTH>(p1, c, pxf, pyf1, m, co, s_rgbd, j, v);
         if (__ballot_sync(0xffffffffu, contrib)) {
           float red = warp_transpose_reduce16(v, lane);
           int k = lane >> 1;
@@ -246,10 +270,7 @@ __global__ void __launch_bounds__(kBwdThreads) k_render_bwd(RenderBwdArgs<Scenes
         if ((s_keep[w][j >> 5] >> (j & 31)) & 1u)
 #pragma unroll
           for (int k = 0; k < 10; ++k) sum[k] += s_part[w][j][k];
-      float4* rec = a.records + (size_t)kRecordFloat4 * s_pidx[threadIdx.x];
-      rec[0] = make_float4(sum[0], sum[1], sum[2], sum[3]);
-      rec[1] = make_float4(sum[4], sum[5], sum[6], sum[7]);
-      rec[2] = make_float4(sum[8], sum[9], 0.f, 0.f);
+      finish_record(a.records + (size_t)kRecordFloat4 * s_pidx[threadIdx.x], sum, s_co[j]);
     }
   }
   for (int i = max_last + threadIdx.x; i < n; i += blockDim.x) {
@@ -262,7 +283,8 @@ __global__ void __launch_bounds__(kBwdThreads) k_render_bwd(RenderBwdArgs<Scenes
 
 template <class Scenes>
 void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st) {
-  k_render_bwd<Scenes><<<tiles, kBwdThreads, 0, st>>>(a);
+  if (a.dL_ddepth) k_render_bwd<Scenes, true><<<tiles, kBwdThreads, 0, st>>>(a);
+  else k_render_bwd<Scenes, false><<<tiles, kBwdThreads, 0, st>>>(a);
 }
 template void launch_render_bwd<SingleScene>(const RenderBwdArgs<SingleScene>&, int, cudaStream_t);
 template void launch_render_bwd<SceneTable>(const RenderBwdArgs<SceneTable>&, int, cudaStream_t);
