@@ -343,6 +343,69 @@ __device__ __forceinline__ float exp_ref_inrange(float x) {
   return p * __int_as_float(((int)kf + 127) << 23);
 }
 
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs: one instruction performs two IEEE round-to-nearest operations
+// (fma/mul/add .rn.f32x2), so each half is bit-identical to the scalar operation. The
+// render kernels evaluate a lane's two pixels with them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long f2_pack(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(f2_pack(a)), "l"(f2_pack(b)), "l"(f2_pack(c)));
+  return f2_unpack(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(d);
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(d);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  unsigned long long d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(d);
+}
+__device__ __forceinline__ float2 splat2(float a) { return make_float2(a, a); }
+
+// gauss_power for the pixels (dx, dy.x) and (dx, dy.y): the same rounding sequence.
+__device__ __forceinline__ float2 gauss_power2(float ca, float cb, float cc, float dx, float2 dy) {
+  float2 e = mul2(splat2(cb), mul2(splat2(dx), dy));
+  e = fma2(mul2(splat2(cc), dy), dy, e);
+  const float cadx = ca * dx;
+  return fma2(splat2(cadx), splat2(dx), e);
+}
+
+// exp_ref_inrange of both halves: the same rounding sequence (fmaf(-k, c, x) is
+// fmaf(k, -c, x) exactly).
+__device__ __forceinline__ float2 exp_ref_inrange2(float2 x) {
+  const float2 t = mul2(x, splat2(1.4426950216293335f));
+  const float2 kf = make_float2(rintf(t.x), rintf(t.y));
+  float2 r = fma2(kf, splat2(-0.693145751953125f), x);
+  r = fma2(kf, splat2(-1.428606765330187e-06f), r);
+  float2 p = fma2(splat2(0.00019841270113829523f), r, splat2(0.0013888889225199819f));
+  p = fma2(p, r, splat2(0.008333333767950535f));
+  p = fma2(p, r, splat2(0.0416666679084301f));
+  p = fma2(p, r, splat2(0.1666666716337204f));
+  p = fma2(p, r, splat2(0.5f));
+  p = fma2(p, r, splat2(1.0f));
+  p = fma2(p, r, splat2(1.0f));
+  const float2 sc = make_float2(__int_as_float(((int)kf.x + 127) << 23), __int_as_float(((int)kf.y + 127) << 23));
+  return mul2(p, sc);
+}
+
 // Lower bound on the exponent of a Gaussian of opacity o that can still give
 // alpha >= 1/255: below it, min(0.99, o exp_ref(power)) < 1/255 for certain, so the
 // pixel can skip the exponential without changing any output. The bound sits 1e-3

@@ -13,34 +13,57 @@ namespace cfgs {
 constexpr int kRenderThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
 constexpr int kRenderBatch = 128;
 
-// Front-to-back state of one pixel and one compositing step (the published loop body,
-// with the exponential skipped below the alpha threshold — exact, see alpha_threshold).
-struct PixelFwd {
-  float T, C0, C1, C2, D;
-  uint32_t last;
-  bool done;
+// Front-to-back state of a lane's two pixels (.x: row r, .y: row r + 4) and one
+// compositing step of both: the published loop body per pixel, with the exponential
+// skipped below the alpha threshold (exact, see alpha_threshold). The arithmetic runs on
+// packed pairs (bit-identical to the scalar operations); each pixel's decisions are its
+// own, and a pixel that does not take the step keeps its state.
+struct PairFwd {
+  float2 T, C0, C1, C2, D;
+  uint32_t last0, last1;
+  bool done0, done1;
 };
 
-__device__ __forceinline__ void composite_step(PixelFwd& p, float pxf, float pyf, const float4& xyt, const float4& co,
+__device__ __forceinline__ void composite_pair(PairFwd& p, float pxf, float2 pyf, const float4& xyt, const float4& co,
                                                const float4* s_rgbd, int j, uint32_t pos1) {
-  if (p.done) return;
-  const float power = gauss_power(co.x, co.y, co.z, xyt.x - pxf, xyt.y - pyf);
-  if (power > 0.0f || power < xyt.z) return;
-  const float alpha = fminf(CFGS_ALPHA_MAX, co.w * exp_ref_inrange(power));
-  if (alpha < CFGS_ALPHA_MIN) return;
-  const float test_T = p.T * (1.0f - alpha);
-  if (test_T < CFGS_T_MIN) {
-    p.done = true;
-    return;
-  }
+  const float2 power = gauss_power2(co.x, co.y, co.z, xyt.x - pxf, sub2(splat2(xyt.y), pyf));
+  bool a0 = !p.done0 && !(power.x > 0.0f || power.x < xyt.z);
+  bool a1 = !p.done1 && !(power.y > 0.0f || power.y < xyt.z);
+  if (!(a0 || a1)) return;
+  float2 alpha = mul2(splat2(co.w), exp_ref_inrange2(power));
+  alpha.x = fminf(CFGS_ALPHA_MAX, alpha.x);
+  alpha.y = fminf(CFGS_ALPHA_MAX, alpha.y);
+  a0 = a0 && !(alpha.x < CFGS_ALPHA_MIN);
+  a1 = a1 && !(alpha.y < CFGS_ALPHA_MIN);
+  if (!(a0 || a1)) return;
+  const float2 test_T = mul2(p.T, sub2(splat2(1.0f), alpha));
+  const bool end0 = a0 && test_T.x < CFGS_T_MIN, end1 = a1 && test_T.y < CFGS_T_MIN;
+  p.done0 = p.done0 || end0;
+  p.done1 = p.done1 || end1;
+  const bool u0 = a0 && !end0, u1 = a1 && !end1;
+  if (!(u0 || u1)) return;
   const float4 c = s_rgbd[j];
-  const float w = alpha * p.T;
-  p.C0 = fmaf(c.x, w, p.C0);
-  p.C1 = fmaf(c.y, w, p.C1);
-  p.C2 = fmaf(c.z, w, p.C2);
-  p.D = fmaf(c.w, w, p.D);
-  p.T = test_T;
-  p.last = pos1;
+  const float2 w = mul2(alpha, p.T);
+  const float2 C0 = fma2(splat2(c.x), w, p.C0);
+  const float2 C1 = fma2(splat2(c.y), w, p.C1);
+  const float2 C2 = fma2(splat2(c.z), w, p.C2);
+  const float2 D = fma2(splat2(c.w), w, p.D);
+  if (u0) {
+    p.C0.x = C0.x;
+    p.C1.x = C1.x;
+    p.C2.x = C2.x;
+    p.D.x = D.x;
+    p.T.x = test_T.x;
+    p.last0 = pos1;
+  }
+  if (u1) {
+    p.C0.y = C0.y;
+    p.C1.y = C1.y;
+    p.C2.y = C2.y;
+    p.D.y = D.y;
+    p.T.y = test_T.y;
+    p.last1 = pos1;
+  }
 }
 
 // One block of 128 threads per 16x16 tile; warp w covers the 8x8 pixel box
@@ -71,10 +94,10 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes
   const float pxf = (float)px, pyf0 = (float)py0, pyf1 = (float)py1;
   const uint32_t lo = a.tile_range[tile];
   const int n = (int)(a.tile_range[tile + 1] - lo);
-  PixelFwd p0{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0u, !in0};
-  PixelFwd p1{1.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0u, !in1};
+  PairFwd pp{splat2(1.0f), splat2(0.0f), splat2(0.0f), splat2(0.0f), splat2(0.0f), 0u, 0u, !in0, !in1};
+  const float2 pyf = make_float2(pyf0, pyf1);
   for (int base = 0; base < n; base += kRenderBatch) {
-    if (__syncthreads_count(p0.done && p1.done) == kRenderThreads) break;
+    if (__syncthreads_count(pp.done0 && pp.done1) == kRenderThreads) break;
     int i = base + threadIdx.x;
     if (i < n) {
       uint32_t g = a.sorted_gid[lo + i];
@@ -100,7 +123,7 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes
     }
 #pragma unroll
     for (int r = 0; r < kRenderBatch / 32; ++r) {
-      if (__all_sync(0xffffffffu, p0.done && p1.done)) break;
+      if (__all_sync(0xffffffffu, pp.done0 && pp.done1)) break;
       uint32_t mk = keep[r];
       while (mk) {
         const int j = r * 32 + __ffs(mk) - 1;
@@ -108,8 +131,7 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes
         const float4 xyt = s_xyt[j];
         const float4 co = s_co[j];
         const uint32_t pos1 = (uint32_t)(base + j + 1);
-        composite_step(p0, pxf, pyf0, xyt, co, s_rgbd, j, pos1);
-        composite_step(p1, pxf, pyf1, xyt, co, s_rgbd, j, pos1);
+        composite_pair(pp, pxf, pyf, xyt, co, s_rgbd, j, pos1);
       }
     }
   }
@@ -117,18 +139,18 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes
   float* col = a.out_color + 3 * (size_t)sd.pix_base;
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
-    const PixelFwd& p = q ? p1 : p0;
     const int py = q ? py1 : py0;
     if (!(q ? in1 : in0)) continue;
+    const float T = q ? pp.T.y : pp.T.x;
     const size_t pix = (size_t)py * sd.W + px;
     const size_t gp = (size_t)sd.pix_base + pix;
-    a.final_T[gp] = p.T;
-    a.n_contrib[gp] = p.last;
-    col[pix] = fmaf(p.T, __ldg(sd.bg + 0), p.C0);
-    col[HW + pix] = fmaf(p.T, __ldg(sd.bg + 1), p.C1);
-    col[2 * HW + pix] = fmaf(p.T, __ldg(sd.bg + 2), p.C2);
-    if (a.out_depth) a.out_depth[gp] = p.D;
-    if (a.out_alpha) a.out_alpha[gp] = 1.0f - p.T;
+    a.final_T[gp] = T;
+    a.n_contrib[gp] = q ? pp.last1 : pp.last0;
+    col[pix] = fmaf(T, __ldg(sd.bg + 0), q ? pp.C0.y : pp.C0.x);
+    col[HW + pix] = fmaf(T, __ldg(sd.bg + 1), q ? pp.C1.y : pp.C1.x);
+    col[2 * HW + pix] = fmaf(T, __ldg(sd.bg + 2), q ? pp.C2.y : pp.C2.x);
+    if (a.out_depth) a.out_depth[gp] = q ? pp.D.y : pp.D.x;
+    if (a.out_alpha) a.out_alpha[gp] = 1.0f - T;
   }
 }
 
