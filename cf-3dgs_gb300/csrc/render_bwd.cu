@@ -19,39 +19,40 @@ constexpr int kBwdBatch = 128;
 constexpr int kBwdThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
 constexpr int kWarps = kBwdThreads / 32;
 
-// Sums 16 per-lane values across the warp in 16 shuffles (instead of 80): each step
-// halves the number of values a lane carries. On return lane L holds the warp total
-// of value index L >> 1.
-__device__ __forceinline__ float warp_transpose_reduce16(float (&v)[16], int lane) {
+// Sums an instance's per-lane terms over the warp. v[0..7] go through a transposing
+// reduction (each step halves the values a lane carries: 4 + 2 + 1 shuffles, then two
+// plain steps), after which lane L holds the total of v[L >> 2]; v[8] (and v[9] with
+// depth gradients) take plain butterflies, every lane ending with the total.
+template <bool DEPTH>
+__device__ __forceinline__ void warp_reduce_terms(float (&v)[10], int lane) {
 #pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    bool up = lane & 16;
-    float send = up ? v[k] : v[k + 8];
-    float keep = up ? v[k + 8] : v[k];
+  for (int k = 0; k < 4; ++k) {
+    const bool up = lane & 16;
+    const float send = up ? v[k] : v[k + 4];
+    const float keep = up ? v[k + 4] : v[k];
     v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
   }
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    bool up = lane & 8;
-    float send = up ? v[k] : v[k + 4];
-    float keep = up ? v[k + 4] : v[k];
+  for (int k = 0; k < 2; ++k) {
+    const bool up = lane & 8;
+    const float send = up ? v[k] : v[k + 2];
+    const float keep = up ? v[k + 2] : v[k];
     v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
   }
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    bool up = lane & 4;
-    float send = up ? v[k] : v[k + 2];
-    float keep = up ? v[k + 2] : v[k];
-    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-  }
   {
-    bool up = lane & 2;
-    float send = up ? v[0] : v[1];
-    float keep = up ? v[1] : v[0];
-    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+    const bool up = lane & 4;
+    const float send = up ? v[0] : v[1];
+    const float keep = up ? v[1] : v[0];
+    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
   }
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
   v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-  return v[0];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v[8] += __shfl_xor_sync(0xffffffffu, v[8], o);
+  if (DEPTH) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[9] += __shfl_xor_sync(0xffffffffu, v[9], o);
+  }
 }
 
 // d/dc of mean |clamp(c, 0, 1) - t| as autograd forms it.
@@ -109,7 +110,7 @@ __device__ __forceinline__ void load_pixel(PixelBwd& p, const RenderBwdArgs<Scen
 // in the forward pass.
 template <bool DEPTH>
 __device__ __forceinline__ bool unwind_step(PixelBwd& p, int c, float pxf, float pyf, const float4& m,
-                                            const float4& co, const float4* s_rgbd, int j, float (&v)[16]) {
+                                            const float4& co, const float4* s_rgbd, int j, float (&v)[10]) {
   if (c >= (int)p.last) return false;
   const float dx = m.x - pxf, dy = m.y - pyf;
   const float power = gauss_power(co.x, co.y, co.z, dx, dy);
@@ -243,17 +244,20 @@ __global__ void __launch_bounds__(kBwdThreads) k_render_bwd(RenderBwdArgs<Scenes
         mk &= ~(1u << bit);
         const int j = r * 32 + bit;
         const int c = base + j;
-        float v[16];
+        float v[10];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) v[k] = 0.f;
+        for (int k = 0; k < 10; ++k) v[k] = 0.f;
         const float4 m = s_xyt[j];
         const float4 co = s_co[j];
         bool contrib = unwind_step<DEPTH>(p0, c, pxf, pyf0, m, co, s_rgbd, j, v);
         contrib |= unwind_step<DEPTH>(p1, c, pxf, pyf1, m, co, s_rgbd, j, v);
         if (__ballot_sync(0xffffffffu, contrib)) {
-          float red = warp_transpose_reduce16(v, lane);
-          int k = lane >> 1;
-          if (!(lane & 1) && k < 10) s_part[warp][j][k] = red;
+          warp_reduce_terms<DEPTH>(v, lane);
+          if ((lane & 3) == 0) s_part[warp][j][lane >> 2] = v[0];
+          if (lane == 0) {
+            s_part[warp][j][8] = v[8];
+            s_part[warp][j][9] = v[9];
+          }
         } else if (lane < 10) {
           s_part[warp][j][lane] = 0.f;
         }
