@@ -51,7 +51,7 @@ struct SortPass {
   int64_t cap;
   int64_t num_chunks;          // chunks covered by the grid
   uint32_t* chunk_counts;      // [1 << bits][num_chunks]
-  uint32_t* digit_totals;      // [1 << bits], zero before the count launch
+  uint32_t* digit_totals;      // [1 << bits], written by the scan
 };
 
 __device__ __forceinline__ uint32_t pass_elements(const SortPass& p) {
@@ -107,7 +107,7 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d, int bits, unsigned a
 }
 
 // Digit histogram of one chunk (per-warp shared-memory counters), written to
-// chunk_counts[d][chunk] and added to digit_totals[d].
+// chunk_counts[d][chunk].
 template <int CHUNK, bool DEPTH>
 __global__ void __launch_bounds__(kSortThreads) k_sort_count(SortPass p) {
   __shared__ uint32_t hist[kSortWarps][kSortDigits];
@@ -136,7 +136,6 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_count(SortPass p) {
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) s += hist[w][d];
     p.chunk_counts[(size_t)d * p.num_chunks + blockIdx.x] = s;
-    if (s) atomicAdd(&p.digit_totals[d], s);
   }
 }
 
@@ -168,20 +167,16 @@ __device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t v, uint32_t* s
   return r;
 }
 
-// One block per digit d: chunk_counts[d][c] becomes the global slot of digit d's first
-// element in chunk c = (elements with a smaller digit) + (digit-d elements of earlier
-// chunks).
+// One block per digit d: chunk_counts[d][c] becomes the number of digit-d elements in
+// earlier chunks, and digit_totals[d] the digit's count. The scatter adds the counts of
+// the smaller digits.
 template <int CHUNK>
 __global__ void __launch_bounds__(1024) k_sort_scan(SortPass p) {
   __shared__ uint32_t sh[64];
   const uint32_t n = pass_elements(p);
-  if (n == 0) return;
   const int d = blockIdx.x;
   const int64_t nc = ((int64_t)n + CHUNK - 1) / CHUNK;
-  uint32_t tot;
-  const uint32_t below = (int)threadIdx.x < d ? p.digit_totals[threadIdx.x] : 0u;
-  block_inclusive_scan(below, sh, &tot);
-  uint32_t carry = tot;
+  uint32_t tot, carry = 0;
   uint32_t* col = p.chunk_counts + (size_t)d * p.num_chunks;
   for (int64_t c0 = 0; c0 < nc; c0 += blockDim.x) {
     const int64_t c = c0 + threadIdx.x;
@@ -190,6 +185,7 @@ __global__ void __launch_bounds__(1024) k_sort_scan(SortPass p) {
     if (c < nc) col[c] = carry + incl - v;
     carry += tot;
   }
+  if (threadIdx.x == 0) p.digit_totals[d] = carry;
 }
 
 // Shared memory of the scatter: keys and payloads in input order, the permutation
@@ -275,9 +271,11 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(SortPass p) {
   }
   uint32_t tot;
   const uint32_t incl = block_inclusive_scan(dsum, sh, &tot);
+  const uint32_t dtot = t < ndig ? p.digit_totals[t] : 0u;
+  const uint32_t below = block_inclusive_scan(dtot, sh, &tot) - dtot;  // elements of smaller digits
   if (t < ndig) {
     s_start[t] = incl - dsum;
-    s_slot[t] = dsum ? p.chunk_counts[(size_t)t * p.num_chunks + blockIdx.x] : 0u;
+    s_slot[t] = dsum ? below + p.chunk_counts[(size_t)t * p.num_chunks + blockIdx.x] : 0u;
   }
   __syncthreads();
 
@@ -463,9 +461,6 @@ template <class Scenes>
 int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {
   const GeomView& gv = a.geom;
   const BinningView& bv = a.bin;
-  if (cudaMemsetAsync(gv.depth_totals, 0, sizeof(uint32_t) * kSortDigits * kDepthPasses, st) != cudaSuccess ||
-      cudaMemsetAsync(bv.totals, 0, sizeof(uint32_t) * kSortDigits * kMaxTilePasses, st) != cudaSuccess)
-    return CFGS_ERR_LAUNCH;
   const int64_t slots = a.total_slots;
   if (slots > 0) {
     // 1. depth sort of the Gaussians: geometry -> 0 -> 1 -> 0 -> depth_val[1]
