@@ -208,6 +208,8 @@ extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   pb.cap = a->capacity;
   pb.counts = v.iv.counts;
   pb.pose_partials = a->pose_partials;
+  pb.flags = &v.iv.counts->flags;
+  pb.sh_bulk = false;  // batched solves carry degree-0 colours
   launch_preprocess_bwd(pb, a->num_blocks, st);
 
   launch_batch_pose_update(a->num_scenes, v.table.d, a->pose_partials, a->xi, a->adam_state,

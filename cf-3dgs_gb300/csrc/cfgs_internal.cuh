@@ -14,6 +14,7 @@ constexpr int kTileY = CFGS_TILE_Y;
 constexpr int kTilePixels = kTileX * kTileY;  // 256
 constexpr int kPreprocessBlock = 256;
 constexpr int kMaxShCoeffs = 16;  // SH degree 3
+#define CFGS_SH_BULK_COEFFS 16
 
 // ---------------------------------------------------------------------------
 // Workspace layouts. Every array starts on a 256-byte boundary.

@@ -97,6 +97,8 @@ struct PreBwdArgs {
   int64_t cap;
   const CfgsCounts* counts;
   double* pose_partials;  // pose-only form: [block][9] float64 sums; NULL for the full backward
+  bool sh_bulk;           // degree-3 SH of each block moved by bulk copies (16-byte aligned arrays)
+  uint32_t* flags;        // CFGS_FLAG_COPY_TIMEOUT
 };
 
 template <class Scenes>

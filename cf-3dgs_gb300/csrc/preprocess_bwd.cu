@@ -67,7 +67,28 @@ __device__ __forceinline__ void sh_backward(int deg, int M, const float* sh, flo
 #pragma unroll
   for (int k = 1; k < 16; ++k)
     if (k >= nb) b[k] = 0.f;
-#define CFGS_SK(k) (sh[3 * (k)] * g0 + sh[3 * (k) + 1] * g1 + sh[3 * (k) + 2] * g2)
+  // s_k = sh_k . g for every coefficient k (12 vector loads when aligned)
+  float sk[16];
+  if (M == 16 && (((uintptr_t)sh) & 15) == 0) {
+    const float4* s4 = reinterpret_cast<const float4*>(sh);
+    const float gc[3] = {g0, g1, g2};
+#pragma unroll
+    for (int k = 0; k < 16; ++k) sk[k] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 12; ++q) {
+      const float4 f = s4[q];
+      const float e[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = 4 * q + u;  // coefficient i / 3, channel i % 3
+        sk[i / 3] = (i % 3 == 0) ? e[u] * gc[0] : sk[i / 3] + e[u] * gc[i % 3];
+      }
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 16; ++k) sk[k] = k < nb ? sh[3 * k] * g0 + sh[3 * k + 1] * g1 + sh[3 * k + 2] * g2 : 0.f;
+  }
+#define CFGS_SK(k) sk[k]
   gdx = gdy = gdz = 0.f;
   if (deg > 0) {
     const float s1 = CFGS_SK(1), s2 = CFGS_SK(2), s3 = CFGS_SK(3);
@@ -115,79 +136,16 @@ __device__ __forceinline__ void sh_backward(int deg, int M, const float* sh, flo
   }
 }
 
-// Full form: all eight gradient arrays. Pose-only form (pose_partials set): only
-// dL/dmean (through projection, covariance and SH view direction) is formed and the
-// block's SE(3) gradient terms — sum g and sum (R p) x g in float64 with the scene's
-// float64 rotation and the un-posed positions p — go to pose_partials[block].
+// The per-Gaussian part of the backward (one thread per Gaussian): record sums acc ->
+// 2D grads, conic -> 2D covariance -> 3D covariance -> scale/rotation, projection ->
+// mean, SH -> coefficients and view direction. SH coefficients are read from sh_src and
+// their gradients written to dsh_dst (NULL: not wanted). Returns dL/dmean in dmean.
 template <class Scenes>
-__global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a) {
-  __shared__ float s_acc[256][11];
-  __shared__ double s_red[8][6];
-  if ((int64_t)a.counts->num_rendered > a.cap) return;  // forward overflowed: outputs untouched
-  const SceneDesc& sd = a.scenes.for_block(blockIdx.x);
-  const bool pose_only = a.pose_partials != nullptr;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t blk0 = (int64_t)blockIdx.x * blockDim.x;
-
-  // ---- phase 1: record sums, eight lanes per Gaussian ------------------------------
-  {
-    const int64_t gl = blk0 + warp * 32 + lane;  // this lane's Gaussian (metadata only)
-    uint32_t nt_l = 0, off_l = 0;
-    if (gl < a.total_slots && gl - sd.gauss_base < sd.num_gaussians && a.radii[gl] > 0) {
-      nt_l = a.geom.touched[gl];
-      off_l = a.geom.offset[gl];
-    }
-    const int sub = lane & 7, grp = lane >> 3;
-#pragma unroll 1
-    for (int gi = 0; gi < 32; gi += 4) {
-      const int src = gi + grp;
-      const uint32_t nt = __shfl_sync(0xffffffffu, nt_l, src);
-      const uint32_t off = __shfl_sync(0xffffffffu, off_l, src);
-      float v[16];
-#pragma unroll
-      for (int k = 0; k < 16; ++k) v[k] = 0.f;
-      for (uint32_t r = sub; r < nt; r += 8) {
-        const float4* rec = a.records + (size_t)kRecordFloat4 * (off + r);
-        const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
-        v[0] += r0.x; v[1] += r0.y; v[2] += r0.z; v[3] += r0.w;
-        v[4] += r1.x; v[5] += r1.y; v[6] += r1.z; v[7] += r1.w;
-        v[8] += r2.x; v[9] += r2.y;
-      }
-      group8_sum16(v, lane);
-      if (sub < 5) {
-        s_acc[warp * 32 + src][2 * sub] = v[0];
-        s_acc[warp * 32 + src][2 * sub + 1] = v[1];
-      }
-    }
-  }
-  __syncthreads();
-
-  // ---- phase 2: one thread per Gaussian ----------------------------------------------
-  const int64_t idx = blk0 + threadIdx.x;
-  if (!pose_only && idx >= a.total_slots) return;
-  const bool valid = idx < a.total_slots && idx - sd.gauss_base < sd.num_gaussians;
+__device__ __forceinline__ void gaussian_backward(const PreBwdArgs<Scenes>& a, const SceneDesc& sd, int64_t idx,
+                                                  uint32_t nt, const float (&acc)[10], const float* sh_src,
+                                                  float* dsh_dst, bool pose_only, float (&dmean)[3]) {
   const int M = sd.sh_coeffs;
-  const uint32_t nt = (valid && a.radii[idx] > 0) ? a.geom.touched[idx] : 0u;
-  float dmean[3] = {0.f, 0.f, 0.f};
-  if (nt == 0 && !pose_only) {
-    for (int k = 0; k < 3; ++k) {
-      a.out.dL_dmeans2D[3 * idx + k] = 0.f;
-      a.out.dL_dcolors[3 * idx + k] = 0.f;
-      a.out.dL_dmeans3D[3 * idx + k] = 0.f;
-      if (a.out.dL_dscales) a.out.dL_dscales[3 * idx + k] = 0.f;
-    }
-    a.out.dL_dopacity[idx] = 0.f;
-    for (int k = 0; k < 6; ++k) a.out.dL_dcov3D[6 * idx + k] = 0.f;
-    if (a.out.dL_drotations)
-      for (int k = 0; k < 4; ++k) a.out.dL_drotations[4 * idx + k] = 0.f;
-    if (a.out.dL_dsh)
-      for (int k = 0; k < 3 * M; ++k) a.out.dL_dsh[(size_t)idx * 3 * M + k] = 0.f;
-    return;
-  }
-  if (nt > 0) {
-    float acc[10];
-#pragma unroll
-    for (int k = 0; k < 10; ++k) acc[k] = s_acc[threadIdx.x][k];
+  {
     const float W = (float)sd.W, H = (float)sd.H;
     const float dndc_x = acc[0] * (0.5f * W), dndc_y = acc[1] * (0.5f * H);
     const float dcol[3] = {acc[6], acc[7], acc[8]};
@@ -334,8 +292,7 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
       const float len = sqrtf(ddx * ddx + ddy * ddy + ddz * ddz);
       const float x = ddx / len, y = ddy / len, z = ddz / len;
       float gdx, gdy, gdz;
-      sh_backward(sd.sh_degree, M, a.g.shs + (size_t)idx * 3 * M, g0, g1, g2, x, y, z,
-                  (!pose_only && a.out.dL_dsh) ? a.out.dL_dsh + (size_t)idx * 3 * M : nullptr, gdx, gdy, gdz);
+      sh_backward(sd.sh_degree, M, sh_src, g0, g1, g2, x, y, z, dsh_dst, gdx, gdy, gdz);
       // d/d(unnormalised direction) = (g - dir (dir . g)) / |d|
       const float dotv = x * gdx + y * gdy + z * gdz;
       dmean[0] += (gdx - x * dotv) / len;
@@ -383,7 +340,152 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
           a.out.dL_drotations[4 * idx + 3] = dq.w;
         }
       }
-      return;
+    }
+  }
+}
+
+// Zero gradients of a Gaussian that touched no tile (full form).
+template <class Scenes>
+__device__ __forceinline__ void zero_gradients(const PreBwdArgs<Scenes>& a, int64_t idx, int M, float* dsh_dst) {
+  for (int k = 0; k < 3; ++k) {
+    a.out.dL_dmeans2D[3 * idx + k] = 0.f;
+    a.out.dL_dcolors[3 * idx + k] = 0.f;
+    a.out.dL_dmeans3D[3 * idx + k] = 0.f;
+    if (a.out.dL_dscales) a.out.dL_dscales[3 * idx + k] = 0.f;
+  }
+  a.out.dL_dopacity[idx] = 0.f;
+  for (int k = 0; k < 6; ++k) a.out.dL_dcov3D[6 * idx + k] = 0.f;
+  if (a.out.dL_drotations)
+    for (int k = 0; k < 4; ++k) a.out.dL_drotations[4 * idx + k] = 0.f;
+  if (dsh_dst)
+    for (int k = 0; k < 3 * M; ++k) dsh_dst[k] = 0.f;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Bounded wait for phase `parity` of an mbarrier; false if it did not complete.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 22); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// Full form: all eight gradient arrays. Pose-only form (pose_partials set): only
+// dL/dmean (through projection, covariance and SH view direction) is formed and the
+// block's SE(3) gradient terms — sum g and sum (R p) x g in float64 with the scene's
+// float64 rotation and the un-posed positions p — go to pose_partials[block].
+// With sh_bulk (degree-3 SH, 16-byte aligned), the block's 256 x 192 bytes of SH
+// coefficients arrive in shared memory by one bulk copy issued before phase 1, and
+// their gradients leave by one bulk store.
+template <class Scenes>
+__global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a) {
+  extern __shared__ __align__(128) float4 s_sh[];  // [256][12] with sh_bulk
+  __shared__ float s_acc[256][11];
+  __shared__ double s_red[8][6];
+  __shared__ __align__(8) uint64_t s_bar;
+  if ((int64_t)a.counts->num_rendered > a.cap) return;  // forward overflowed: outputs untouched
+  const SceneDesc& sd = a.scenes.for_block(blockIdx.x);
+  const bool pose_only = a.pose_partials != nullptr;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t blk0 = (int64_t)blockIdx.x * blockDim.x;
+  const int M = sd.sh_coeffs;
+  const bool bulk = a.sh_bulk && a.g.shs != nullptr && M == kMaxShCoeffs;
+  const uint32_t in_block = (uint32_t)min((int64_t)blockDim.x, a.total_slots - blk0);
+  const uint32_t sh_bytes = in_block * 3u * kMaxShCoeffs * (uint32_t)sizeof(float);
+  const uint32_t bar = smem_addr(&s_bar);
+  if (bulk) {
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(sh_bytes) : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       smem_addr(s_sh)),
+                   "l"(a.g.shs + (size_t)blk0 * 3 * kMaxShCoeffs), "r"(sh_bytes), "r"(bar)
+                   : "memory");
+    }
+  }
+
+  // ---- phase 1: record sums, eight lanes per Gaussian ------------------------------
+  {
+    const int64_t gl = blk0 + warp * 32 + lane;  // this lane's Gaussian (metadata only)
+    uint32_t nt_l = 0, off_l = 0;
+    if (gl < a.total_slots && gl - sd.gauss_base < sd.num_gaussians && a.radii[gl] > 0) {
+      nt_l = a.geom.touched[gl];
+      off_l = a.geom.offset[gl];
+    }
+    const int sub = lane & 7, grp = lane >> 3;
+#pragma unroll 1
+    for (int gi = 0; gi < 32; gi += 4) {
+      const int src = gi + grp;
+      const uint32_t nt = __shfl_sync(0xffffffffu, nt_l, src);
+      const uint32_t off = __shfl_sync(0xffffffffu, off_l, src);
+      float v[16];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) v[k] = 0.f;
+      for (uint32_t r = sub; r < nt; r += 8) {
+        const float4* rec = a.records + (size_t)kRecordFloat4 * (off + r);
+        const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
+        v[0] += r0.x; v[1] += r0.y; v[2] += r0.z; v[3] += r0.w;
+        v[4] += r1.x; v[5] += r1.y; v[6] += r1.z; v[7] += r1.w;
+        v[8] += r2.x; v[9] += r2.y;
+      }
+      group8_sum16(v, lane);
+      if (sub < 5) {
+        s_acc[warp * 32 + src][2 * sub] = v[0];
+        s_acc[warp * 32 + src][2 * sub + 1] = v[1];
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- phase 2: one thread per Gaussian ----------------------------------------------
+  bool sh_ready = true;
+  if (bulk) {
+    sh_ready = mbar_wait(bar, 0);
+    if (!sh_ready) atomicOr(a.flags, CFGS_FLAG_COPY_TIMEOUT);
+  }
+  const int64_t idx = blk0 + threadIdx.x;
+  const bool valid = idx < a.total_slots && idx - sd.gauss_base < sd.num_gaussians;
+  const uint32_t nt = (valid && a.radii[idx] > 0) ? a.geom.touched[idx] : 0u;
+  const bool want_dsh = !pose_only && a.out.dL_dsh != nullptr;
+  float* own_sh = reinterpret_cast<float*>(s_sh + 12 * threadIdx.x);
+  const float* sh_src = nullptr;
+  float* dsh_dst = nullptr;
+  if (idx < a.total_slots && a.g.shs) {
+    sh_src = bulk && sh_ready ? own_sh : a.g.shs + (size_t)idx * 3 * M;
+    if (want_dsh) dsh_dst = bulk ? own_sh : a.out.dL_dsh + (size_t)idx * 3 * M;
+  }
+  float dmean[3] = {0.f, 0.f, 0.f};
+  if (idx < a.total_slots) {
+    if (nt > 0) {
+      float acc[10];
+#pragma unroll
+      for (int k = 0; k < 10; ++k) acc[k] = s_acc[threadIdx.x][k];
+      gaussian_backward(a, sd, idx, nt, acc, sh_src, dsh_dst, pose_only, dmean);
+    } else if (!pose_only) {
+      zero_gradients(a, idx, M, dsh_dst);
+    }
+  }
+  if (bulk && want_dsh) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(
+                       a.out.dL_dsh + (size_t)blk0 * 3 * kMaxShCoeffs),
+                   "r"(smem_addr(s_sh)), "r"(sh_bytes)
+                   : "memory");
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
     }
   }
   if (!pose_only) return;
@@ -421,7 +523,13 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
 
 template <class Scenes>
 void launch_preprocess_bwd(const PreBwdArgs<Scenes>& a, int blocks, cudaStream_t st) {
-  k_preprocess_bwd<Scenes><<<blocks, 256, 0, st>>>(a);
+  constexpr int kShBulkBytes = 256 * 3 * kMaxShCoeffs * (int)sizeof(float);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_preprocess_bwd<Scenes>, cudaFuncAttributeMaxDynamicSharedMemorySize, kShBulkBytes);
+    attr_set = true;
+  }
+  k_preprocess_bwd<Scenes><<<blocks, 256, a.sh_bulk ? kShBulkBytes : 0, st>>>(a);
 }
 template void launch_preprocess_bwd<SingleScene>(const PreBwdArgs<SingleScene>&, int, cudaStream_t);
 template void launch_preprocess_bwd<SceneTable>(const PreBwdArgs<SceneTable>&, int, cudaStream_t);

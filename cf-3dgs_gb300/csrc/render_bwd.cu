@@ -359,6 +359,9 @@ extern "C" int cfgs_preprocess_backward(const CfgsSettings* s, const CfgsGaussia
   pa.cap = capacity;
   pa.counts = iv.counts;
   pa.pose_partials = nullptr;
+  pa.flags = &iv.counts->flags;
+  pa.sh_bulk = g->shs != nullptr && g->sh_coeffs == CFGS_SH_BULK_COEFFS && (((uintptr_t)g->shs) & 15) == 0 &&
+               (out->dL_dsh == nullptr || (((uintptr_t)out->dL_dsh) & 15) == 0);
   launch_preprocess_bwd(pa, div_up(g->num_gaussians, 256), st);
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;

@@ -46,6 +46,8 @@ typedef enum CfgsStatus {
 /* Bits of CfgsCounts.flags (raised by kernels, read back with cfgs_read_counts). */
 #define CFGS_FLAG_FRUSTUM_VIOLATION 0x1u /* prefiltered=1 but a point was at view z <= 0.2 */
 #define CFGS_FLAG_CAPACITY_OVERFLOW 0x2u /* K > binning capacity; outputs are invalid      */
+#define CFGS_FLAG_COPY_TIMEOUT 0x4u      /* a bounded wait for an on-chip copy ran out;   */
+                                         /* that call's outputs are invalid               */
 
 /* Tile size of the screen-space binning (pixels). */
 #define CFGS_TILE_X 16
