@@ -175,7 +175,7 @@ __device__ __forceinline__ void finish_record(float4* rec, const float (&s)[10],
 // warp reduction; the cross-warp sum of an instance adds only the warps that kept it
 // (the others' terms are exact zeros).
 template <class Scenes, bool DEPTH>
-__global__ void __launch_bounds__(kBwdThreads) k_render_bwd(RenderBwdArgs<Scenes> a) {
+__global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Scenes> a) {
   __shared__ float4 s_xyt[kBwdBatch];
   __shared__ float4 s_co[kBwdBatch];
   __shared__ float4 s_rgbd[kBwdBatch];
