@@ -133,10 +133,11 @@ def _peaks() -> dict:
         return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from the ncu
-# captures summarised in profiles/<kernel>_1M_1080p.md, at the instance count K they were
-# taken at; scaled by instances for another K.
-NCU_TRAFFIC = {"render_bwd": (300232960 + 630901760, 12433348)}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
+# capture of the 1M-Gaussian 1080p workload (profiles/traffic_1M_1080p.md), at the
+# instance count K it was taken at; scaled by instances for another K.
+NCU_TRAFFIC = {"render_bwd": (362095616 + 673941760, 12433348),
+               "composite": (66856960 + 28301824, 12433348)}
 
 
 def _traffic(kernel: str, K: int):
