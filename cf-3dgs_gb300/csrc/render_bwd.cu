@@ -62,11 +62,9 @@ __device__ __forceinline__ float l1_grad(float c, float t, float inv_numel) {
   return (c >= 0.0f && c <= 1.0f) ? inv_numel * sgn : 0.0f;
 }
 
-// Back-to-front state of one pixel: its upstream gradients, the transmittance being
-// unwound and the running colour/depth behind the current instance.
+// Forward results and upstream gradients of one pixel.
 struct PixelBwd {
   float T_final, dC0, dC1, dC2, dD, dA_bg;  // dA_bg = dL/dalpha - bg . dL/dcolor
-  float T, acc0, acc1, acc2, accd, last_a, last0, last1, last2, lastd;
   uint32_t last;
 };
 
@@ -97,61 +95,95 @@ __device__ __forceinline__ void load_pixel(PixelBwd& p, const RenderBwdArgs<Scen
     }
   }
   p.dA_bg = dA - (__ldg(sd.bg + 0) * p.dC0 + __ldg(sd.bg + 1) * p.dC1 + __ldg(sd.bg + 2) * p.dC2);
-  p.T = p.T_final;
-  p.acc0 = p.acc1 = p.acc2 = p.accd = 0.f;
-  p.last_a = p.last0 = p.last1 = p.last2 = p.lastd = 0.f;
 }
 
-// Unwinds one instance at list position c for one pixel and adds its terms to v:
+// Back-to-front state of a lane's two pixels (.x: row r, .y: row r + 4): upstream
+// gradients, the transmittance being unwound, and the colour/depth accumulated behind the
+// current instance (updated right after each contributing instance, which gives the
+// value upstream forms from the previous instance's alpha and colour).
+struct PairBwd {
+  float2 T_final, dC0, dC1, dC2, dD, dA_bg;
+  float2 T, acc0, acc1, acc2, accd;
+  uint32_t last0, last1;
+};
+
+__device__ __forceinline__ PairBwd make_pair(const PixelBwd& p, const PixelBwd& q) {
+  PairBwd P;
+  P.T_final = make_float2(p.T_final, q.T_final);
+  P.dC0 = make_float2(p.dC0, q.dC0);
+  P.dC1 = make_float2(p.dC1, q.dC1);
+  P.dC2 = make_float2(p.dC2, q.dC2);
+  P.dD = make_float2(p.dD, q.dD);
+  P.dA_bg = make_float2(p.dA_bg, q.dA_bg);
+  P.T = P.T_final;
+  P.acc0 = P.acc1 = P.acc2 = P.accd = make_float2(0.f, 0.f);
+  P.last0 = p.last;
+  P.last1 = q.last;
+  return P;
+}
+
+// Unwinds one instance at list position c for both pixels and adds their terms to v:
 // with g = G dL/dalpha (G the Gaussian's value at the pixel, d = mean - pixel),
 // v0..v4 += g (dx, dy, dx^2, dx dy, dy^2), v5 += g, v6..v8 += w dL/drgb, v9 += w
 // dL/ddepth (w = alpha T). The per-instance factors (opacity, conic) are applied after
-// the reduction (finish_record). Returns whether the instance contributed to the pixel
-// in the forward pass.
+// the reduction (finish_record). A pixel the instance did not reach in the forward pass
+// keeps its state: its factors are 1 (transmittance) and 0 (alpha, G). Returns whether
+// the instance contributed to either pixel.
 template <bool DEPTH>
-__device__ __forceinline__ bool unwind_step(PixelBwd& p, int c, float pxf, float pyf, const float4& m,
-                                            const float4& co, const float4* s_rgbd, int j, float (&v)[10]) {
-  if (c >= (int)p.last) return false;
-  const float dx = m.x - pxf, dy = m.y - pyf;
-  const float power = gauss_power(co.x, co.y, co.z, dx, dy);
-  if (power > 0.0f || power < m.z) return false;
-  const float G = exp_ref_inrange(power);
-  const float alpha = fminf(CFGS_ALPHA_MAX, co.w * G);
-  if (alpha < CFGS_ALPHA_MIN) return false;
+__device__ __forceinline__ bool unwind_pair(PairBwd& P, int c, float pxf, float2 pyf, const float4& m, const float4& co,
+                                            const float4* s_rgbd, int j, float (&v)[10]) {
+  const bool in0 = c < (int)P.last0, in1 = c < (int)P.last1;
+  if (!(in0 || in1)) return false;
+  const float dx = m.x - pxf;
+  const float2 dy = sub2(splat2(m.y), pyf);
+  const float2 power = gauss_power2(co.x, co.y, co.z, dx, dy);
+  bool a0 = in0 && !(power.x > 0.0f || power.x < m.z);
+  bool a1 = in1 && !(power.y > 0.0f || power.y < m.z);
+  if (!(a0 || a1)) return false;
+  const float2 G = exp_ref_inrange2(power);
+  float2 alpha = mul2(splat2(co.w), G);
+  alpha.x = fminf(CFGS_ALPHA_MAX, alpha.x);
+  alpha.y = fminf(CFGS_ALPHA_MAX, alpha.y);
+  a0 = a0 && !(alpha.x < CFGS_ALPHA_MIN);
+  a1 = a1 && !(alpha.y < CFGS_ALPHA_MIN);
+  if (!(a0 || a1)) return false;
   const float4 col = s_rgbd[j];
-  float inv_one_m;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(inv_one_m) : "f"(1.0f - alpha));
-  p.T = p.T * inv_one_m;
-  const float w = alpha * p.T;
-  v[6] = fmaf(p.dC0, w, v[6]);
-  v[7] = fmaf(p.dC1, w, v[7]);
-  v[8] = fmaf(p.dC2, w, v[8]);
-  p.acc0 = fmaf(p.last_a, p.last0 - p.acc0, p.acc0);
-  p.acc1 = fmaf(p.last_a, p.last1 - p.acc1, p.acc1);
-  p.acc2 = fmaf(p.last_a, p.last2 - p.acc2, p.acc2);
-  float dLda = (col.x - p.acc0) * p.dC0;
-  dLda = fmaf(col.y - p.acc1, p.dC1, dLda);
-  dLda = fmaf(col.z - p.acc2, p.dC2, dLda);
+  const float2 om = sub2(splat2(1.0f), alpha);
+  float r0, r1;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(om.x));
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(om.y));
+  const float2 inv = make_float2(a0 ? r0 : 1.0f, a1 ? r1 : 1.0f);
+  const float2 am = make_float2(a0 ? alpha.x : 0.0f, a1 ? alpha.y : 0.0f);
+  P.T = mul2(P.T, inv);
+  const float2 w = mul2(am, P.T);
+  v[6] = fmaf(P.dC0.y, w.y, fmaf(P.dC0.x, w.x, v[6]));
+  v[7] = fmaf(P.dC1.y, w.y, fmaf(P.dC1.x, w.x, v[7]));
+  v[8] = fmaf(P.dC2.y, w.y, fmaf(P.dC2.x, w.x, v[8]));
+  const float2 e0 = sub2(splat2(col.x), P.acc0), e1 = sub2(splat2(col.y), P.acc1), e2 = sub2(splat2(col.z), P.acc2);
+  float2 dLda = mul2(e0, P.dC0);
+  dLda = fma2(e1, P.dC1, dLda);
+  dLda = fma2(e2, P.dC2, dLda);
+  P.acc0 = fma2(am, e0, P.acc0);
+  P.acc1 = fma2(am, e1, P.acc1);
+  P.acc2 = fma2(am, e2, P.acc2);
   if (DEPTH) {
-    v[9] = fmaf(p.dD, w, v[9]);
-    p.accd = fmaf(p.last_a, p.lastd - p.accd, p.accd);
-    dLda = fmaf(col.w - p.accd, p.dD, dLda);
-    p.lastd = col.w;
+    v[9] = fmaf(P.dD.y, w.y, fmaf(P.dD.x, w.x, v[9]));
+    const float2 ed = sub2(splat2(col.w), P.accd);
+    dLda = fma2(ed, P.dD, dLda);
+    P.accd = fma2(am, ed, P.accd);
   }
-  p.last0 = col.x;
-  p.last1 = col.y;
-  p.last2 = col.z;
-  p.last_a = alpha;
-  dLda *= p.T;
-  dLda = fmaf(p.T_final * inv_one_m, p.dA_bg, dLda);
-  const float g = G * dLda;  // d/d opacity (straight through the 0.99 clamp)
-  v[5] += g;
-  const float gx = g * dx, gy = g * dy;
-  v[0] += gx;
-  v[1] += gy;
-  v[2] = fmaf(gx, dx, v[2]);
-  v[3] = fmaf(gx, dy, v[3]);
-  v[4] = fmaf(gy, dy, v[4]);
+  dLda = mul2(dLda, P.T);
+  dLda = fma2(mul2(P.T_final, inv), P.dA_bg, dLda);
+  const float2 g = mul2(make_float2(a0 ? G.x : 0.0f, a1 ? G.y : 0.0f), dLda);  // d/d opacity
+  const float sg = g.x + g.y;
+  v[5] += sg;
+  const float sx = sg * dx;  // both pixels share dx
+  const float2 gy = mul2(g, dy);
+  v[0] += sx;
+  v[1] += gy.x + gy.y;
+  v[2] = fmaf(sx, dx, v[2]);
+  v[3] = fmaf(g.y * dx, dy.y, fmaf(g.x * dx, dy.x, v[3]));
+  v[4] = fmaf(gy.y, dy.y, fmaf(gy.x, dy.x, v[4]));
   return true;
 }
 
@@ -200,6 +232,8 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
   PixelBwd p0, p1;
   load_pixel(p0, a, sd, in0, in0 ? (size_t)py0 * sd.W + px : 0);
   load_pixel(p1, a, sd, in1, in1 ? (size_t)py1 * sd.W + px : 0);
+  PairBwd pp = make_pair(p0, p1);
+  const float2 pyf = make_float2(pyf0, pyf1);
   if (threadIdx.x == 0) s_max = 0;
   __syncthreads();
   const uint32_t my_last = max(p0.last, p1.last);
@@ -249,8 +283,7 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
         for (int k = 0; k < 10; ++k) v[k] = 0.f;
         const float4 m = s_xyt[j];
         const float4 co = s_co[j];
-        bool contrib = unwind_step<DEPTH>(p0, c, pxf, pyf0, m, co, s_rgbd, j, v);
-        contrib |= unwind_step<DEPTH>(p1, c, pxf, pyf1, m, co, s_rgbd, j, v);
+        const bool contrib = unwind_pair<DEPTH>(pp, c, pxf, pyf, m, co, s_rgbd, j, v);
         if (__ballot_sync(0xffffffffu, contrib)) {
           warp_reduce_terms<DEPTH>(v, lane);
           if ((lane & 3) == 0) s_part[warp][j][lane >> 2] = v[0];
