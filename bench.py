@@ -43,7 +43,7 @@ def _args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
-    p.add_argument("--workload", default="fwdbwd", choices=["fwdbwd", "pose", "batch", "serve"])
+    p.add_argument("--workload", default="fwdbwd", choices=["fwdbwd", "pose", "batch", "serve", "ssim"])
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--serve-seconds", type=float, default=60.0)
     p.add_argument("--serve-slots", type=int, default=64)
@@ -487,6 +487,71 @@ def run_serve(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_ssim(a) -> None:
+    """SSIM loss (the pose loss's 0.2 (1 - SSIM) term, utils/loss_utils.py:33-58) on a
+    3x1080x1920 image pair, forward + backward per step: the fused kernels vs the
+    reference's formulation in PyTorch (depthwise conv2d + autograd) on the same GPU."""
+    import torch
+    import torch.nn.functional as F
+    from cfgs import ssim as ssim_mod
+    dev = torch.device("cuda", 0)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    C, H, W = 3, 1080, 1920
+    x0 = torch.rand(C, H, W, generator=g).to(dev)
+    y = (x0 + 0.1 * torch.randn(C, H, W, generator=g).to(dev)).clamp(0, 1)
+    w1 = torch.exp(-((torch.arange(11, dtype=torch.float64) - 5) ** 2) / (2 * 1.5 ** 2))
+    w1 = (w1 / w1.sum()).float()
+    win = (w1[:, None] @ w1[None, :]).expand(C, 1, 11, 11).contiguous().to(dev)
+
+    def torch_ssim(x):
+        xb, yb = x[None], y[None]
+        mu1, mu2 = F.conv2d(xb, win, padding=5, groups=C), F.conv2d(yb, win, padding=5, groups=C)
+        s11 = F.conv2d(xb * xb, win, padding=5, groups=C) - mu1 * mu1
+        s22 = F.conv2d(yb * yb, win, padding=5, groups=C) - mu2 * mu2
+        s12 = F.conv2d(xb * yb, win, padding=5, groups=C) - mu1 * mu2
+        m = ((2 * mu1 * mu2 + 1e-4) * (2 * s12 + 9e-4)) / ((mu1 * mu1 + mu2 * mu2 + 1e-4) * (s11 + s22 + 9e-4))
+        return m.mean()
+
+    def timed(fn, steps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for _ in range(a.warmup):
+            fn()
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(steps):
+            fn()
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / steps
+
+    def step(f):
+        x = x0.clone().requires_grad_(True)
+        (0.2 * (1.0 - f(x))).backward()
+        return x.grad
+
+    def fused_ssim(x):
+        return ssim_mod.ssim(x, y)
+
+    ms_fused = timed(lambda: step(fused_ssim), a.steps)
+    ms_torch = timed(lambda: step(torch_ssim), max(3, a.steps // 4))
+    gf, gt = step(fused_ssim), step(torch_ssim)
+    rel = float((gf - gt).abs().max() / gt.abs().max())
+    vf, vt = float(ssim_mod.ssim(x0, y)), float(torch_ssim(x0))
+    n = C * H * W
+    algo = 4 * n * (2 + 3 + 3 + 2 + 1)  # fwd: read 2 images, write 3 maps; bwd: read 3 maps + 2 images, write 1
+    peaks = _peaks()
+    achieved = algo / (ms_fused / 1000.0) / 1e9
+    line = {"metric": "SSIM loss fwd+bwd per s (3x1080x1920)", "value": round(1000.0 / ms_fused, 3),
+            "unit": "steps/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "0.2 (1 - SSIM) of a 3x1080x1920 image pair, 11x11 window, fwd + bwd"},
+            "ms_per_step": round(ms_fused, 4), "torch_ms_per_step": round(ms_torch, 4),
+            "speedup_vs_torch": round(ms_torch / ms_fused, 3),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": round(achieved / peaks["hbm_gbs"], 5), "algorithmic_bytes": algo},
+            "ssim_fused": vf, "ssim_torch": vt, "grad_max_rel_diff_vs_torch": rel}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
@@ -497,6 +562,8 @@ def main():
         run_batch(a)
     elif a.workload == "serve":
         run_serve(a)
+    elif a.workload == "ssim":
+        run_ssim(a)
     else:
         run_ours(a)
 

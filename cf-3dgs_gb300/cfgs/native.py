@@ -124,6 +124,9 @@ EXPORTS = {
     "cfgs_pose_scratch_bytes": (C.c_size_t, [C.c_int32]),
     "cfgs_pose_grad": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_pose_adam": (C.c_int, [C.c_int32, _vp, _vp, _vp, C.c_double, C.c_double, C.c_double, C.c_double, _vp]),
+    "cfgs_ssim_scratch_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
+    "cfgs_ssim_forward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp]),
+    "cfgs_ssim_backward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_batch_plan": (C.c_int, [C.c_int32, C.POINTER(BatchScene), _vp, C.POINTER(BatchPlan), _vp, _vp, _vp, _vp,
                                   _vp, _vp]),
     "cfgs_batch_init": (C.c_int, [C.POINTER(BatchArgs), _vp]),

@@ -1,0 +1,262 @@
+// Fused SSIM (structural similarity) with an 11x11 Gaussian window, forward and
+// backward, as the CF-3DGS pose loss uses it: utils/loss_utils.py:23-58 and
+// trainer/losses.py:147-251 (window sigma 1.5, zero padding 5, one window per channel,
+// C1 = 0.01^2, C2 = 0.03^2, mean over every channel and pixel).
+//
+// Per channel and pixel p the five windowed moments mu1 = W*x, mu2 = W*y, exx = W*x^2,
+// eyy = W*y^2, exy = W*xy give
+//   S = (2 mu1 mu2 + C1)(2 s12 + C2) / ((mu1^2 + mu2^2 + C1)(s11 + s22 + C2)),
+//   s11 = exx - mu1^2, s22 = eyy - mu2^2, s12 = exy - mu1 mu2.
+// The forward writes, besides the partial sums of S, the three maps
+//   a = dS/dmu1, b = dS/dexx, c = dS/dexy    (times 1/count: d mean / d S_p)
+// and the backward forms dL/dx_q = g (W*a + 2 x_q W*b + y_q W*c)_q with g = dL/dmean
+// (the window is symmetric, so the transposed convolution is the same convolution).
+//
+// Both kernels work on 32x16 output tiles of one channel: the tile and a 5-pixel halo
+// are staged in shared memory (zero outside the image), a horizontal 11-tap pass runs
+// over all staged rows, then a vertical 11-tap pass per output pixel.
+#include <cmath>
+
+#include "cfgs_internal.cuh"
+
+namespace cfgs {
+
+constexpr int kSsimR = 5;  // window radius
+constexpr int kSsimTaps = 2 * kSsimR + 1;
+constexpr int kSsimTW = 32, kSsimTH = 16;
+constexpr int kSsimSW = kSsimTW + 2 * kSsimR, kSsimSH = kSsimTH + 2 * kSsimR;  // staged tile
+constexpr int kSsimThreads = 256;
+constexpr float kSsimC1 = 0.0001f, kSsimC2 = 0.0009f;
+
+__constant__ float c_ssim_w[kSsimTaps];
+
+struct SsimDims {
+  int C, H, W, tiles_x, tiles_y;
+};
+
+__device__ __forceinline__ float load_or_zero(const float* img, int H, int W, int y, int x) {
+  return (y >= 0 && y < H && x >= 0 && x < W) ? img[(size_t)y * W + x] : 0.0f;
+}
+
+// Block-wide sum of one double per thread (kSsimThreads threads), fixed order.
+__device__ __forceinline__ double block_sum_fixed(double v, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kSsimThreads / 32; ++w) t += sh[w];
+  return t;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(kSsimThreads) k_ssim_fwd(SsimDims d, const float* __restrict__ img1,
+                                                           const float* __restrict__ img2, float* __restrict__ maps,
+                                                           double* __restrict__ partials, float inv_count) {
+  __shared__ float s_x[kSsimSH][kSsimSW], s_y[kSsimSH][kSsimSW];
+  __shared__ float s_h[5][kSsimSH][kSsimTW];  // horizontal sums of x, y, xx, yy, xy
+  __shared__ double s_red[kSsimThreads / 32];
+  const int tile = blockIdx.x, ch = blockIdx.y;
+  const int x0 = (tile % d.tiles_x) * kSsimTW, y0 = (tile / d.tiles_x) * kSsimTH;
+  const size_t plane = (size_t)d.H * d.W;
+  const float* X = img1 + ch * plane;
+  const float* Y = img2 + ch * plane;
+  for (int i = threadIdx.x; i < kSsimSH * kSsimSW; i += kSsimThreads) {
+    const int r = i / kSsimSW, c = i % kSsimSW;
+    s_x[r][c] = load_or_zero(X, d.H, d.W, y0 + r - kSsimR, x0 + c - kSsimR);
+    s_y[r][c] = load_or_zero(Y, d.H, d.W, y0 + r - kSsimR, x0 + c - kSsimR);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kSsimSH * kSsimTW; i += kSsimThreads) {
+    const int r = i / kSsimTW, c = i % kSsimTW;
+    float hx = 0.f, hy = 0.f, hxx = 0.f, hyy = 0.f, hxy = 0.f;
+#pragma unroll
+    for (int k = 0; k < kSsimTaps; ++k) {
+      const float w = c_ssim_w[k], u = s_x[r][c + k], v = s_y[r][c + k];
+      hx = fmaf(w, u, hx);
+      hy = fmaf(w, v, hy);
+      hxx = fmaf(w, u * u, hxx);
+      hyy = fmaf(w, v * v, hyy);
+      hxy = fmaf(w, u * v, hxy);
+    }
+    s_h[0][r][c] = hx;
+    s_h[1][r][c] = hy;
+    s_h[2][r][c] = hxx;
+    s_h[3][r][c] = hyy;
+    s_h[4][r][c] = hxy;
+  }
+  __syncthreads();
+  double ssum = 0.0;
+  for (int i = threadIdx.x; i < kSsimTH * kSsimTW; i += kSsimThreads) {
+    const int r = i / kSsimTW, c = i % kSsimTW;
+    const int py = y0 + r, px = x0 + c;
+    if (py >= d.H || px >= d.W) continue;
+    float mu1 = 0.f, mu2 = 0.f, exx = 0.f, eyy = 0.f, exy = 0.f;
+#pragma unroll
+    for (int k = 0; k < kSsimTaps; ++k) {
+      const float w = c_ssim_w[k];
+      mu1 = fmaf(w, s_h[0][r + k][c], mu1);
+      mu2 = fmaf(w, s_h[1][r + k][c], mu2);
+      exx = fmaf(w, s_h[2][r + k][c], exx);
+      eyy = fmaf(w, s_h[3][r + k][c], eyy);
+      exy = fmaf(w, s_h[4][r + k][c], exy);
+    }
+    const float m11 = mu1 * mu1, m22 = mu2 * mu2, m12 = mu1 * mu2;
+    const float A = 2.f * m12 + kSsimC1, B = 2.f * (exy - m12) + kSsimC2;
+    const float Cc = m11 + m22 + kSsimC1, D = (exx - m11) + (eyy - m22) + kSsimC2;
+    const float S = (A * B) / (Cc * D);
+    ssum += (double)S;
+    const size_t q = ch * plane + (size_t)py * d.W + px;
+    // dS/dmu1 = S (2 mu2/A - 2 mu2/B - 2 mu1/C + 2 mu1/D); dS/dexx = -S/D; dS/dexy = 2 S/B
+    const float da = S * (2.f * mu2 * (1.f / A - 1.f / B) + 2.f * mu1 * (1.f / D - 1.f / Cc));
+    maps[q] = inv_count * da;
+    maps[(size_t)d.C * plane + q] = inv_count * (-S / D);
+    maps[2 * (size_t)d.C * plane + q] = inv_count * (2.f * S / B);
+  }
+  const double t = block_sum_fixed(ssum, s_red);
+  if (threadIdx.x == 0) partials[(size_t)ch * gridDim.x + tile] = t;
+}
+
+// Mean SSIM from the per-tile partial sums, in a fixed order (one block).
+__global__ void __launch_bounds__(kSsimThreads) k_ssim_mean(const double* __restrict__ partials, int count,
+                                                            double inv_count, float* __restrict__ out) {
+  __shared__ double s_red[kSsimThreads / 32];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < count; i += kSsimThreads) v += partials[i];
+  const double t = block_sum_fixed(v, s_red);
+  if (threadIdx.x == 0) *out = (float)(t * inv_count);
+}
+
+__global__ void __launch_bounds__(kSsimThreads) k_ssim_bwd(SsimDims d, const float* __restrict__ img1,
+                                                           const float* __restrict__ img2,
+                                                           const float* __restrict__ maps,
+                                                           const float* __restrict__ dL_dmean,
+                                                           float* __restrict__ dL_dimg1) {
+  __shared__ float s_m[3][kSsimSH][kSsimSW];
+  __shared__ float s_h[3][kSsimSH][kSsimTW];
+  const int tile = blockIdx.x, ch = blockIdx.y;
+  const int x0 = (tile % d.tiles_x) * kSsimTW, y0 = (tile / d.tiles_x) * kSsimTH;
+  const size_t plane = (size_t)d.H * d.W;
+  for (int i = threadIdx.x; i < kSsimSH * kSsimSW; i += kSsimThreads) {
+    const int r = i / kSsimSW, c = i % kSsimSW;
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+      s_m[m][r][c] =
+          load_or_zero(maps + ((size_t)m * d.C + ch) * plane, d.H, d.W, y0 + r - kSsimR, x0 + c - kSsimR);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kSsimSH * kSsimTW; i += kSsimThreads) {
+    const int r = i / kSsimTW, c = i % kSsimTW;
+    float h0 = 0.f, h1 = 0.f, h2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < kSsimTaps; ++k) {
+      const float w = c_ssim_w[k];
+      h0 = fmaf(w, s_m[0][r][c + k], h0);
+      h1 = fmaf(w, s_m[1][r][c + k], h1);
+      h2 = fmaf(w, s_m[2][r][c + k], h2);
+    }
+    s_h[0][r][c] = h0;
+    s_h[1][r][c] = h1;
+    s_h[2][r][c] = h2;
+  }
+  __syncthreads();
+  const float g = *dL_dmean;
+  for (int i = threadIdx.x; i < kSsimTH * kSsimTW; i += kSsimThreads) {
+    const int r = i / kSsimTW, c = i % kSsimTW;
+    const int py = y0 + r, px = x0 + c;
+    if (py >= d.H || px >= d.W) continue;
+    float va = 0.f, vb = 0.f, vc = 0.f;
+#pragma unroll
+    for (int k = 0; k < kSsimTaps; ++k) {
+      const float w = c_ssim_w[k];
+      va = fmaf(w, s_h[0][r + k][c], va);
+      vb = fmaf(w, s_h[1][r + k][c], vb);
+      vc = fmaf(w, s_h[2][r + k][c], vc);
+    }
+    const size_t q = ch * plane + (size_t)py * d.W + px;
+    dL_dimg1[q] = g * (va + 2.f * img1[q] * vb + img2[q] * vc);
+  }
+}
+
+namespace {
+
+// The window (utils/loss_utils.py:23-29: exp(-(x - 5)^2 / (2 sigma^2)), sigma 1.5,
+// normalised to sum 1) goes to constant memory once per device.
+bool upload_window(cudaStream_t st) {
+  constexpr int kMaxDevices = 64;
+  static bool done[kMaxDevices] = {};
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return false;
+  if (done[dev]) return true;
+  double g[kSsimTaps], sum = 0.0;
+  for (int k = 0; k < kSsimTaps; ++k) {
+    const double t = (double)(k - kSsimR);
+    g[k] = std::exp(-t * t / (2.0 * 1.5 * 1.5));
+    sum += g[k];
+  }
+  float w[kSsimTaps];
+  for (int k = 0; k < kSsimTaps; ++k) w[k] = (float)(g[k] / sum);
+  if (cudaMemcpyToSymbolAsync(c_ssim_w, w, sizeof(w), 0, cudaMemcpyHostToDevice, st) != cudaSuccess) return false;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return false;
+  done[dev] = true;
+  return true;
+}
+
+SsimDims dims(int32_t C, int32_t H, int32_t W) {
+  SsimDims d;
+  d.C = C;
+  d.H = H;
+  d.W = W;
+  d.tiles_x = (W + kSsimTW - 1) / kSsimTW;
+  d.tiles_y = (H + kSsimTH - 1) / kSsimTH;
+  return d;
+}
+
+bool dims_ok(int32_t C, int32_t H, int32_t W) {
+  return C > 0 && H > 0 && W > 0 && C <= 65535 && (int64_t)C * H * W <= ((int64_t)1 << 31);
+}
+
+}  // namespace
+
+}  // namespace cfgs
+
+using namespace cfgs;
+
+extern "C" size_t cfgs_ssim_scratch_bytes(int32_t channels, int32_t height, int32_t width) {
+  if (!dims_ok(channels, height, width)) return 0;
+  const SsimDims d = dims(channels, height, width);
+  const size_t maps = sizeof(float) * 3 * (size_t)channels * height * width;
+  const size_t parts = sizeof(double) * (size_t)channels * d.tiles_x * d.tiles_y;
+  return align256(maps) + align256(parts);
+}
+
+extern "C" int cfgs_ssim_forward(int32_t channels, int32_t height, int32_t width, const float* img1,
+                                 const float* img2, void* scratch, float* ssim_mean, void* stream) {
+  if (!dims_ok(channels, height, width) || !img1 || !img2 || !scratch || !ssim_mean) return CFGS_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!upload_window(st)) return CFGS_ERR_LAUNCH;
+  const SsimDims d = dims(channels, height, width);
+  const size_t count = (size_t)channels * height * width;
+  float* maps = static_cast<float*>(scratch);
+  double* parts = reinterpret_cast<double*>(static_cast<char*>(scratch) + align256(sizeof(float) * 3 * count));
+  const int tiles = d.tiles_x * d.tiles_y;
+  k_ssim_fwd<<<dim3(tiles, channels), kSsimThreads, 0, st>>>(d, img1, img2, maps, parts, (float)(1.0 / (double)count));
+  k_ssim_mean<<<1, kSsimThreads, 0, st>>>(parts, tiles * channels, 1.0 / (double)count, ssim_mean);
+  CFGS_CHECK_LAUNCH(0, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_ssim_backward(int32_t channels, int32_t height, int32_t width, const float* img1,
+                                  const float* img2, const void* scratch, const float* dL_dmean, float* dL_dimg1,
+                                  void* stream) {
+  if (!dims_ok(channels, height, width) || !img1 || !img2 || !scratch || !dL_dmean || !dL_dimg1)
+    return CFGS_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!upload_window(st)) return CFGS_ERR_LAUNCH;
+  const SsimDims d = dims(channels, height, width);
+  k_ssim_bwd<<<dim3(d.tiles_x * d.tiles_y, channels), kSsimThreads, 0, st>>>(
+      d, img1, img2, static_cast<const float*>(scratch), dL_dmean, dL_dimg1);
+  CFGS_CHECK_LAUNCH(0, st);
+  return CFGS_OK;
+}

@@ -248,6 +248,21 @@ int cfgs_pose_grad(int32_t num_points, const float* xi, const float* xyz,
 int cfgs_pose_adam(int32_t count, float* xi, const float* grad, float* state, double lr,
                    double beta1, double beta2, double eps, void* stream);
 
+/* ---- SSIM loss (pose-solve photometric loss) ---------------------------------------
+ * Mean structural similarity of img1 against img2 ([C,H,W] float32, device), 11x11
+ * Gaussian window (sigma 1.5), zero padding, one window per channel, C1 = 0.01^2,
+ * C2 = 0.03^2: the ssim() of utils/loss_utils.py:33-58 and the _ssim of
+ * trainer/losses.py:147-196 (size_average, no mask), which CF-3DGS weights as
+ * (1 - lambda) L1 + lambda (1 - SSIM) (trainer/losses.py:98-136).
+ * cfgs_ssim_forward writes the mean to ssim_mean (device float) and keeps in `scratch`
+ * (cfgs_ssim_scratch_bytes) what the backward needs; cfgs_ssim_backward writes
+ * dL/dimg1 = dL_dmean[0] * d mean / d img1 (img2 gets no gradient). Deterministic. */
+size_t cfgs_ssim_scratch_bytes(int32_t channels, int32_t height, int32_t width);
+int cfgs_ssim_forward(int32_t channels, int32_t height, int32_t width, const float* img1, const float* img2,
+                      void* scratch, float* ssim_mean, void* stream);
+int cfgs_ssim_backward(int32_t channels, int32_t height, int32_t width, const float* img1, const float* img2,
+                       const void* scratch, const float* dL_dmean, float* dL_dimg1, void* stream);
+
 /* ---- batched pose solves ----------------------------------------------------------
  * Many CF-3DGS pose solves (trainer/cf3dgs_trainer.py:261-285), each with its own
  * Gaussians, camera and resolution, advance together: one call runs one Adam iteration

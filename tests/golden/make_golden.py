@@ -10,7 +10,9 @@ or in CFGS_REFERENCE) on seeded inputs:
   (scene/gaussian_model_cf.py:834-838);
 - scene/cameras.py Camera (intrinsics branch) with utils/graphics_utils.py
   getWorld2View3: world_view_transform, full_proj_transform, camera_center;
-- utils/graphics_utils.py getProjectionMatrix / fov2focal / focal2fov.
+- utils/graphics_utils.py getProjectionMatrix / fov2focal / focal2fov;
+- utils/loss_utils.py ssim (the pose loss's SSIM term) on seeded image pairs, with
+  autograd's gradient with respect to the first image.
 
 The reference writes device='cuda' into some tensor constructors and calls .cuda();
 this script runs them on the CPU by dropping those device arguments. Run:
@@ -100,6 +102,20 @@ for i in range(4):
 P = graphics_utils.getProjectionMatrix(0.01, 100.0, 1.1, 0.8)
 out["projmatrix_fov"] = P.numpy()
 out["fov2focal"] = np.array([graphics_utils.fov2focal(1.1, 640), graphics_utils.focal2fov(500.0, 640)])
+
+# SSIM (utils/loss_utils.py:33-58), float64, gradient by autograd
+from utils import loss_utils  # noqa: E402
+for i, (C, H, W) in enumerate([(3, 24, 31), (1, 13, 9), (3, 40, 64)]):
+    a = rng.uniform(0, 1, (C, H, W))
+    b = np.clip(a + rng.normal(0, 0.15, (C, H, W)), 0, 1) if i != 1 else rng.uniform(0, 1, (C, H, W))
+    x = torch.tensor(a[None], dtype=torch.float64, requires_grad=True)
+    win = loss_utils.create_window(11, C).double()
+    v = loss_utils._ssim(x, torch.tensor(b[None], dtype=torch.float64), win, 11, C, True)
+    v.backward()
+    out[f"ssim{i}_img1"] = a.astype(np.float32)
+    out[f"ssim{i}_img2"] = b.astype(np.float32)
+    out[f"ssim{i}_value"] = np.array(v.item())
+    out[f"ssim{i}_grad"] = x.grad[0].numpy()
 
 dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_math.npz")
 np.savez_compressed(dst, **out)

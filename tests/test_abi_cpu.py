@@ -83,3 +83,12 @@ def test_dropin_validates_argument_combinations():
     assert dgr.GaussianRasterizationSettings._fields == (
         "image_height", "image_width", "tanfovx", "tanfovy", "bg", "scale_modifier", "viewmatrix", "projmatrix",
         "sh_degree", "campos", "prefiltered", "debug")
+
+
+def test_ssim_abi_host_checks():
+    from cfgs import native
+    lib = native.load()
+    assert lib.cfgs_ssim_scratch_bytes(3, 360, 640) >= 3 * 3 * 360 * 640 * 4
+    assert lib.cfgs_ssim_scratch_bytes(0, 10, 10) == 0
+    assert lib.cfgs_ssim_forward(3, 0, 10, None, None, None, None, None) == 1
+    assert lib.cfgs_ssim_backward(3, 10, 10, None, None, None, None, None, None) == 1

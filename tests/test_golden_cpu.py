@@ -68,3 +68,16 @@ def test_camera_matches_reference(g, i):
     np.testing.assert_allclose(cam.projmatrix.numpy(), g[f"cam{i}_full"], rtol=0, atol=1e-5)
     np.testing.assert_allclose(cam.campos.numpy(), g[f"cam{i}_center"], rtol=0, atol=1e-5)
     np.testing.assert_allclose([cam.tanfovx, cam.tanfovy], g[f"cam{i}_tanfov"], rtol=1e-7)
+
+
+def test_ssim_oracle_matches_reference():
+    """oracle/ssim_oracle.py against the reference's utils/loss_utils.py ssim (value and
+    autograd gradient, float64) on the golden image pairs."""
+    from oracle import ssim_oracle
+    g = np.load(GOLD)
+    for i in range(3):
+        v, grad = ssim_oracle.ssim(g[f"ssim{i}_img1"], g[f"ssim{i}_img2"], with_grad=True)
+        # the reference's window is rounded to float32 (utils/loss_utils.py:27-28)
+        assert abs(v - float(g[f"ssim{i}_value"])) < 1e-6
+        ref = g[f"ssim{i}_grad"]
+        assert np.abs(grad - ref).max() <= 1e-5 * np.abs(ref).max()
