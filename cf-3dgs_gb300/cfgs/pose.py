@@ -251,8 +251,42 @@ def l1(img: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
     return (img.clamp(0, 1) - target).abs().mean()
 
 
-def solve(prob: PoseProblem, iters: int = 300, lr: float = 1e-3, mode: str = "fused", record: bool = False):
-    """Runs the pose solve; returns (xi [6] float64 numpy, losses list if record)."""
+def ssim_torch(img1: torch.Tensor, img2: torch.Tensor) -> torch.Tensor:
+    """The reference's SSIM in PyTorch (utils/loss_utils.py:23-58: 11x11 Gaussian window,
+    sigma 1.5, depthwise conv2d with zero padding 5): the plain path's SSIM."""
+    import torch.nn.functional as F
+    C = img1.shape[-3]
+    w1 = torch.exp(-((torch.arange(11, dtype=torch.float64) - 5) ** 2) / (2 * 1.5 ** 2))
+    w1 = (w1 / w1.sum()).to(img1)
+    win = (w1[:, None] @ w1[None, :]).expand(C, 1, 11, 11).contiguous()
+    x, y = img1.reshape(1, C, *img1.shape[-2:]), img2.reshape(1, C, *img2.shape[-2:])
+    mu1, mu2 = F.conv2d(x, win, padding=5, groups=C), F.conv2d(y, win, padding=5, groups=C)
+    s11 = F.conv2d(x * x, win, padding=5, groups=C) - mu1 * mu1
+    s22 = F.conv2d(y * y, win, padding=5, groups=C) - mu2 * mu2
+    s12 = F.conv2d(x * y, win, padding=5, groups=C) - mu1 * mu2
+    c1, c2 = 0.01 ** 2, 0.03 ** 2
+    return (((2 * mu1 * mu2 + c1) * (2 * s12 + c2)) / ((mu1 * mu1 + mu2 * mu2 + c1) * (s11 + s22 + c2))).mean()
+
+
+def photometric_loss(img: torch.Tensor, target: torch.Tensor, lambda_dssim: float, fused: bool) -> torch.Tensor:
+    """(1 - lambda) L1 + lambda (1 - SSIM) of the clamped render (trainer/losses.py:98-136;
+    CF-3DGS uses lambda_dssim = 0.2). lambda 0 is the RGB L1 alone."""
+    if lambda_dssim == 0.0:
+        return l1(img, target)
+    c = img.clamp(0, 1)
+    if fused:
+        from .ssim import ssim
+        s = ssim(c, target)
+    else:
+        s = ssim_torch(c, target)
+    return (1.0 - lambda_dssim) * (c - target).abs().mean() + lambda_dssim * (1.0 - s)
+
+
+def solve(prob: PoseProblem, iters: int = 300, lr: float = 1e-3, mode: str = "fused", record: bool = False,
+          lambda_dssim: float = 0.0):
+    """Runs the pose solve; returns (xi [6] float64 numpy, losses list if record).
+    lambda_dssim > 0 adds the SSIM term of the reference's loss (PyTorch SSIM on the
+    plain path, the fused SSIM kernels on the fused path)."""
     dev = prob.xyz.device
     losses = []
     if mode == "plain":
@@ -260,7 +294,7 @@ def solve(prob: PoseProblem, iters: int = 300, lr: float = 1e-3, mode: str = "fu
         opt = torch.optim.Adam([xi], lr=lr, eps=1e-15)
         for _ in range(iters):
             means, _ = apply_pose_torch(xi, prob.xyz)
-            loss = l1(render(prob, means), prob.target)
+            loss = photometric_loss(render(prob, means), prob.target, lambda_dssim, fused=False)
             loss.backward()
             opt.step()
             opt.zero_grad(set_to_none=True)
@@ -273,7 +307,7 @@ def solve(prob: PoseProblem, iters: int = 300, lr: float = 1e-3, mode: str = "fu
         for _ in range(iters):
             xi_leaf = xi.detach().requires_grad_(True)
             means = pose_apply(xi_leaf, prob.xyz)
-            loss = l1(render(prob, means), prob.target)
+            loss = photometric_loss(render(prob, means), prob.target, lambda_dssim, fused=True)
             loss.backward()
             opt.step(xi_leaf.grad)
             if record:
