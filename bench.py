@@ -43,7 +43,7 @@ def _args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
-    p.add_argument("--workload", default="fwdbwd", choices=["fwdbwd", "pose", "batch", "serve", "ssim"])
+    p.add_argument("--workload", default="fwdbwd", choices=["fwdbwd", "pose", "batch", "serve", "ssim", "init"])
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--serve-seconds", type=float, default=60.0)
     p.add_argument("--serve-slots", type=int, default=64)
@@ -570,6 +570,76 @@ def run_ssim(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_init(a) -> None:
+    """Local-Gaussian initialisation of one frame (the steps before each pose solve):
+    640x360 depth -> points -> 0.01 voxel down-sampling -> three-nearest-neighbour
+    scales -> initial Gaussians, and the kNN step alone on 1,000,000 points. CPU
+    comparison on the host cores: the C restatement of the voxel step and scipy's
+    k-d tree for the neighbours."""
+    import time
+    import numpy as np
+    import torch
+    from cfgs import pointcloud
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(0)
+    v, u = np.mgrid[0:360, 0:640].astype(np.float32)
+    depth = (2.0 + 0.5 * np.sin(u / 37.0) + 0.3 * np.cos(v / 23.0) + 0.02 * rng.standard_normal((360, 640)))
+    depth = depth.astype(np.float32)
+    rgb = rng.uniform(0, 1, (360 * 640, 3)).astype(np.float32)
+    K = np.array([[500.0, 0, 320.0], [0, 500.0, 180.0], [0, 0, 1]])
+    d_dev, rgb_dev = torch.tensor(depth, device=dev), torch.tensor(rgb, device=dev)
+
+    def frame():
+        pts = pointcloud.depth_to_points(d_dev, K)
+        p, c = pointcloud.voxel_down_sample(pts, rgb_dev, 0.01)
+        return pointcloud.gaussians_from_points(p, c)
+
+    for _ in range(a.warmup):
+        g = frame()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        g = frame()
+    torch.cuda.synchronize()
+    ms_frame = (time.perf_counter() - t0) * 1000.0 / a.steps
+    n_vox = int(g["xyz"].shape[0])
+    big = torch.randn(1_000_000, 3, device=dev)
+    for _ in range(a.warmup):
+        pointcloud.dist_cuda2(big)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(a.steps):
+        pointcloud.dist_cuda2(big)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_knn = ev0.elapsed_time(ev1) / a.steps
+    cpu = {}
+    if not a.no_cpu:
+        from oracle import c_oracle
+        pts_h = pointcloud.depth_to_points(d_dev, K).cpu().numpy()
+        t0 = time.perf_counter()
+        vp, vc = c_oracle.voxel_down_sample(pts_h, rgb, 0.01)
+        cpu["voxel_ms_c_1thread"] = round((time.perf_counter() - t0) * 1000.0, 2)
+        try:
+            from scipy.spatial import cKDTree
+            t0 = time.perf_counter()
+            cKDTree(vp.astype(np.float64)).query(vp.astype(np.float64), k=4, workers=-1)
+            cpu["knn_frame_ms_scipy"] = round((time.perf_counter() - t0) * 1000.0, 2)
+            bh = big.cpu().numpy().astype(np.float64)
+            t0 = time.perf_counter()
+            cKDTree(bh).query(bh, k=4, workers=-1)
+            cpu["knn_1M_ms_scipy"] = round((time.perf_counter() - t0) * 1000.0, 2)
+        except ImportError:
+            pass
+        cpu["cores"] = len(os.sched_getaffinity(0))
+    line = {"metric": "frame initialisations/s (640x360 depth -> local Gaussians)", "value": round(1000.0 / ms_frame, 3),
+            "unit": "frames/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "depth_to_points + voxel_down_sample(0.01) + distCUDA2 scales + create_from_pcd, "
+                                   "640x360", "points": 640 * 360, "voxels": n_vox},
+            "ms_per_frame": round(ms_frame, 4), "knn_1M_points_ms": round(ms_knn, 4), "cpu": cpu}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = _args()
     if a.impl == "reference":
@@ -582,6 +652,8 @@ def main():
         run_serve(a)
     elif a.workload == "ssim":
         run_ssim(a)
+    elif a.workload == "init":
+        run_init(a)
     else:
         run_ours(a)
 

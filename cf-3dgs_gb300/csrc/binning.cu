@@ -532,6 +532,39 @@ int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {
   return CFGS_OK;
 }
 template int launch_binning<SingleScene>(const BinArgs<SingleScene>&, cudaStream_t);
+
+// Stable LSD radix sort of n (key, value) pairs by the low `bits` key bits, passes of at
+// most 8 bits, ping-ponging between (keys[0], vals[0]) and (keys[1], vals[1]); returns
+// the index (0 or 1) of the buffers holding the result. chunk_counts holds
+// 256 x sort_chunks(n, kTileChunk) values, totals 256 x kMaxTilePasses.
+int sort_pairs(uint32_t* keys[2], uint32_t* vals[2], int64_t n, int bits, uint32_t* chunk_counts, uint32_t* totals,
+               cudaStream_t st, int* result) {
+  if (bits < 1 || bits > 32 || n < 0 || n > 0x7fffffffll) return CFGS_ERR_INVALID_ARGUMENT;
+  const int passes = (bits + 7) / 8;
+  const int width = (bits + passes - 1) / passes;
+  int src = 0;
+  for (int pass = 0; pass < passes; ++pass) {
+    SortPass p{};
+    const int dst = src ^ 1;
+    p.key_in = keys[src];
+    p.val_in = vals[src];
+    p.key_out = keys[dst];
+    p.val_out = vals[dst];
+    p.shift = width * pass;
+    p.bits = min(width, bits - width * pass);
+    p.n = n;
+    p.cap = n;
+    p.num_chunks = sort_chunks(n, kTileChunk);
+    p.chunk_counts = chunk_counts;
+    p.digit_totals = totals + kSortDigits * pass;
+    int s = launch_pass<kTileChunk, false>(p, st);
+    if (s != CFGS_OK) return s;
+    src = dst;
+  }
+  *result = src;
+  return CFGS_OK;
+}
+
 template int launch_binning<SceneTable>(const BinArgs<SceneTable>&, cudaStream_t);
 
 }  // namespace cfgs

@@ -263,6 +263,24 @@ int cfgs_ssim_forward(int32_t channels, int32_t height, int32_t width, const flo
 int cfgs_ssim_backward(int32_t channels, int32_t height, int32_t width, const float* img1, const float* img2,
                        const void* scratch, const float* dL_dmean, float* dL_dimg1, void* stream);
 
+/* ---- frame initialisation (local Gaussians before each pose solve) ---------------------
+ * kornia depth_to_3d (normalize_points=False; trainer/trainer.py:491): [H,W] depth ->
+ * [H*W,3] camera-space points ((u - cx)/fx * d, (v - cy)/fy * d, d), row-major pixels. */
+int cfgs_depth_to_points(int32_t height, int32_t width, const float* depth, float fx, float fy, float cx, float cy,
+                         float* xyz, void* stream);
+/* Device workspace of the two point-cloud operations below for num_points points. */
+size_t cfgs_pointcloud_workspace_bytes(int64_t num_points);
+/* simple-knn distCUDA2 (scene/gaussian_model_cf.py:194): dist2[i] = mean of the squared
+ * distances from point i to its three nearest other points (FLT_MAX for missing ones).
+ * Exact (Morton-ordered boxes with bounded pruning). */
+int cfgs_knn3_mean_dist2(int64_t num_points, const float* xyz, void* workspace, float* dist2, void* stream);
+/* Open3D voxel_down_sample (trainer/trainer.py:507): points (and colours, may be NULL)
+ * of each occupied voxel floor((p - (min - s/2)) / s) averaged in float64 in input
+ * order; out_xyz/out_rgb need room for num_points rows; *num_voxels receives the count
+ * (voxels in increasing linear voxel index order). Synchronises `stream`. */
+int cfgs_voxel_down_sample(int64_t num_points, const float* xyz, const float* rgb, double voxel_size,
+                           void* workspace, float* out_xyz, float* out_rgb, int64_t* num_voxels, void* stream);
+
 /* ---- batched pose solves ----------------------------------------------------------
  * Many CF-3DGS pose solves (trainer/cf3dgs_trainer.py:261-285), each with its own
  * Gaussians, camera and resolution, advance together: one call runs one Adam iteration

@@ -178,3 +178,47 @@ class Oracle:
                                      _p(out["means3D"], _fp), _p(out["cov3D"], _fp), _p(out["sh"], _fp),
                                      _p(out["scales"], _fp), _p(out["rotations"], _fp))
         return out
+
+
+# ---- frame initialisation (oracle/pointcloud_oracle.c) ----------------------------------
+def _pc_lib():
+    L = lib()
+    if not getattr(L, "_pc_ready", False):
+        L.oracle_depth_to_points.restype = None
+        L.oracle_depth_to_points.argtypes = [C.c_int, C.c_int, _fp, C.c_float, C.c_float, C.c_float, C.c_float, _fp]
+        L.oracle_knn3_mean_dist2.restype = None
+        L.oracle_knn3_mean_dist2.argtypes = [C.c_int64, _fp, _fp]
+        L.oracle_voxel_down_sample.restype = C.c_int64
+        L.oracle_voxel_down_sample.argtypes = [C.c_int64, _fp, _fp, C.c_double, _fp, _fp]
+        L._pc_ready = True
+    return L
+
+
+def _f32c(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+
+
+def depth_to_points(depth, fx, fy, cx, cy):
+    d = _f32c(depth)
+    H, W = d.shape
+    out = np.empty((H * W, 3), np.float32)
+    _pc_lib().oracle_depth_to_points(H, W, d.ctypes.data_as(_fp), fx, fy, cx, cy, out.ctypes.data_as(_fp))
+    return out
+
+
+def knn3_mean_dist2(points):
+    p = _f32c(points).reshape(-1, 3)
+    out = np.empty(p.shape[0], np.float32)
+    _pc_lib().oracle_knn3_mean_dist2(p.shape[0], p.ctypes.data_as(_fp), out.ctypes.data_as(_fp))
+    return out
+
+
+def voxel_down_sample(points, colors, voxel_size):
+    p = _f32c(points).reshape(-1, 3)
+    c = None if colors is None else _f32c(colors).reshape(-1, 3)
+    op = np.empty_like(p)
+    oc = None if c is None else np.empty_like(c)
+    m = _pc_lib().oracle_voxel_down_sample(p.shape[0], p.ctypes.data_as(_fp),
+                                           None if c is None else c.ctypes.data_as(_fp), float(voxel_size),
+                                           op.ctypes.data_as(_fp), None if oc is None else oc.ctypes.data_as(_fp))
+    return op[:m], (None if oc is None else oc[:m])

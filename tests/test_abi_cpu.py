@@ -92,3 +92,17 @@ def test_ssim_abi_host_checks():
     assert lib.cfgs_ssim_scratch_bytes(0, 10, 10) == 0
     assert lib.cfgs_ssim_forward(3, 0, 10, None, None, None, None, None) == 1
     assert lib.cfgs_ssim_backward(3, 10, 10, None, None, None, None, None, None) == 1
+
+
+def test_pointcloud_abi_host_checks():
+    from cfgs import native
+    lib = native.load()
+    assert lib.cfgs_pointcloud_workspace_bytes(1000) > 1000 * 16
+    assert lib.cfgs_pointcloud_workspace_bytes(-1) == 0
+    assert lib.cfgs_depth_to_points(0, 4, None, 1.0, 1.0, 0.0, 0.0, None, None) == 1
+    assert lib.cfgs_knn3_mean_dist2(-1, None, None, None, None) == 1
+    assert lib.cfgs_knn3_mean_dist2(0, None, None, None, None) == 0
+    m = native.C.c_int64(7)
+    assert lib.cfgs_voxel_down_sample(10, None, None, 0.0, None, None, None, native.C.byref(m), None) == 1
+    assert lib.cfgs_voxel_down_sample(0, None, None, 0.01, None, None, None, native.C.byref(m), None) == 0
+    assert m.value == 0
