@@ -15,7 +15,7 @@
 
 namespace cfgs {
 
-constexpr int kBwdBatch = 128;
+constexpr int kBwdBatch = 64;
 constexpr int kBwdThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
 constexpr int kWarps = kBwdThreads / 32;
 
