@@ -16,6 +16,7 @@
 namespace cfgs {
 
 constexpr int kBwdBatch = 64;
+static_assert(kBwdBatch % 32 == 0, "batches are whole ballot words");
 constexpr int kBwdThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
 constexpr int kWarps = kBwdThreads / 32;
 
