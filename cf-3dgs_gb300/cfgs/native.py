@@ -124,6 +124,14 @@ EXPORTS = {
     "cfgs_pose_scratch_bytes": (C.c_size_t, [C.c_int32]),
     "cfgs_pose_grad": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_pose_adam": (C.c_int, [C.c_int32, _vp, _vp, _vp, C.c_double, C.c_double, C.c_double, C.c_double, _vp]),
+    "cfgs_gaussian_adam": (C.c_int, [C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_double, C.c_double,
+                                     C.c_int64, _vp]),
+    "cfgs_densify_stats": (C.c_int, [C.c_int64, _vp, _vp, _vp, _vp, _vp]),
+    "cfgs_densify_workspace_bytes": (C.c_size_t, [C.c_int64]),
+    "cfgs_densify_plan": (C.c_int, [C.c_int64, _vp, _vp, _vp, _vp, C.c_float, C.c_float, C.c_float, C.c_float,
+                                    C.c_int32, _vp, _vp, _vp]),
+    "cfgs_densify_write": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, C.c_int32, _vp, _vp, _vp, _vp,
+                                     _vp]),
     "cfgs_depth_to_points": (C.c_int, [C.c_int32, C.c_int32, _vp, C.c_float, C.c_float, C.c_float, C.c_float, _vp,
                                        _vp]),
     "cfgs_pointcloud_workspace_bytes": (C.c_size_t, [C.c_int64]),

@@ -281,6 +281,35 @@ int cfgs_knn3_mean_dist2(int64_t num_points, const float* xyz, void* workspace, 
 int cfgs_voxel_down_sample(int64_t num_points, const float* xyz, const float* rgb, double voxel_size,
                            void* workspace, float* out_xyz, float* out_rgb, int64_t* num_voxels, void* stream);
 
+/* ---- Gaussian-parameter optimisation (global refinement, local fitting) ------------------
+ * torch.optim.Adam over the parameter groups of GaussianModel.training_setup
+ * (scene/gaussian_model_cf.py:242-266; eps 1e-15) in one launch: group k has numel[k]
+ * float32 elements at params[k] with gradients grads[k] and moments exp_avg[k],
+ * exp_avg_sq[k], learning rate lr[k]; `step` is the step count after this step. The
+ * operation sequence is torch's multi-tensor Adam, so results are bit-identical. */
+int cfgs_gaussian_adam(int32_t num_groups, float* const* params, const float* const* grads, float* const* exp_avg,
+                       float* const* exp_avg_sq, const int64_t* numel, const double* lr, double beta1, double beta2,
+                       double eps, int64_t step, void* stream);
+/* add_densification_stats (scene/gaussian_model_cf.py:716-719) with the visibility filter
+ * radii > 0: grad_accum += |dL/dmeans2D[:, :2]|, denom += 1. */
+int cfgs_densify_stats(int64_t num_gaussians, const int32_t* radii, const float* grad_means2D, float* grad_accum,
+                       float* denom, void* stream);
+/* densify_and_prune (scene/gaussian_model_cf.py:628-694), in two steps. cfgs_densify_plan
+ * classifies every Gaussian and returns counts = {kept originals, kept clones, split
+ * points, kept children per copy} (synchronises `stream`); cfgs_densify_write then writes
+ * one array of the new model, rows = counts[0] + counts[1] + 2 counts[3] in the
+ * reference's order (kept originals, kept clones, children copy 0, children copy 1):
+ * role 0 copies a parameter array of `width` floats per row, 1 an Adam moment (zero for
+ * new rows), 2 the positions and 3 the scalings (split children computed from xyz,
+ * scaling, rotation and the standard-normal draws z [2][counts[2]][3]). */
+size_t cfgs_densify_workspace_bytes(int64_t num_gaussians);
+int cfgs_densify_plan(int64_t num_gaussians, const float* grad_accum, const float* denom, const float* scaling,
+                      const float* opacity, float max_grad, float min_opacity, float extent, float percent_dense,
+                      int32_t prune_big, void* workspace, int64_t counts[4], void* stream);
+int cfgs_densify_write(int64_t num_gaussians, void* workspace, const int64_t counts[4], int32_t width,
+                       const float* in, float* out, int32_t role, const float* xyz, const float* scaling,
+                       const float* rotation, const float* z, void* stream);
+
 /* ---- batched pose solves ----------------------------------------------------------
  * Many CF-3DGS pose solves (trainer/cf3dgs_trainer.py:261-285), each with its own
  * Gaussians, camera and resolution, advance together: one call runs one Adam iteration
