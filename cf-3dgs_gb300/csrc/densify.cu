@@ -35,7 +35,8 @@ struct AdamGroups {
   const float* g[kMaxAdamGroups];
   float* m[kMaxAdamGroups];
   float* v[kMaxAdamGroups];
-  int64_t begin[kMaxAdamGroups + 1];  // flattened element ranges
+  int64_t begin[kMaxAdamGroups + 1];  // flattened ranges of 4-element items
+  int64_t numel[kMaxAdamGroups];
   float step_size[kMaxAdamGroups];    // -lr / bc1
   float bc2_sqrt[kMaxAdamGroups];
   float eps[kMaxAdamGroups];
@@ -43,22 +44,50 @@ struct AdamGroups {
   int count;
 };
 
-__global__ void __launch_bounds__(256) k_gaussian_adam(AdamGroups a) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.begin[a.count]) return;
-  int k = 0;
-  while (k + 1 < a.count && i >= a.begin[k + 1]) ++k;
-  const int64_t e = i - a.begin[k];
-  const float g = a.g[k][e];
-  float m = a.m[k][e], v = a.v[k][e];
+__device__ __forceinline__ void adam_elem(const AdamGroups& a, int k, float g, float& m, float& v, float& p) {
   m = fmaf(a.w1, g - m, m);
   v = v * a.b2;
   v = fmaf(a.w2, g * g, v);
-  a.m[k][e] = m;
-  a.v[k][e] = v;
   float denom = sqrtf(v) / a.bc2_sqrt[k];
   denom = denom + a.eps[k];
-  a.p[k][e] = fmaf(a.step_size[k], m / denom, a.p[k][e]);
+  p = fmaf(a.step_size[k], m / denom, p);
+}
+
+// One thread per 4 consecutive elements of a group (begin[] counts 4-element items, each
+// group padded to a whole item): vector loads and stores where the item is whole and the
+// arrays 16-byte aligned, scalar ones otherwise.
+__global__ void __launch_bounds__(256) k_gaussian_adam(AdamGroups a) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.begin[a.count]) return;
+  int k = 0;
+  while (k + 1 < a.count && t >= a.begin[k + 1]) ++k;
+  const int64_t e0 = 4 * (t - a.begin[k]);
+  const int64_t numel = a.numel[k];
+  float* P = a.p[k];
+  const float* G = a.g[k];
+  float* Mv = a.m[k];
+  float* Vv = a.v[k];
+  const bool vec = e0 + 3 < numel && ((((uintptr_t)P) | ((uintptr_t)G) | ((uintptr_t)Mv) | ((uintptr_t)Vv)) & 15) == 0;
+  if (vec) {
+    const float4 g4 = *reinterpret_cast<const float4*>(G + e0);
+    float4 m4 = *reinterpret_cast<float4*>(Mv + e0), v4 = *reinterpret_cast<float4*>(Vv + e0);
+    float4 p4 = *reinterpret_cast<float4*>(P + e0);
+    adam_elem(a, k, g4.x, m4.x, v4.x, p4.x);
+    adam_elem(a, k, g4.y, m4.y, v4.y, p4.y);
+    adam_elem(a, k, g4.z, m4.z, v4.z, p4.z);
+    adam_elem(a, k, g4.w, m4.w, v4.w, p4.w);
+    *reinterpret_cast<float4*>(Mv + e0) = m4;
+    *reinterpret_cast<float4*>(Vv + e0) = v4;
+    *reinterpret_cast<float4*>(P + e0) = p4;
+  } else {
+    for (int64_t e = e0; e < min(numel, e0 + 4); ++e) {
+      float m = Mv[e], v = Vv[e], p = P[e];
+      adam_elem(a, k, G[e], m, v, p);
+      Mv[e] = m;
+      Vv[e] = v;
+      P[e] = p;
+    }
+  }
 }
 
 // xyz_gradient_accum[i] += |grad2D[i, :2]|, denom[i] += 1 where radii[i] > 0
@@ -111,43 +140,93 @@ __global__ void __launch_bounds__(256) k_densify_classify(int64_t n, const float
   cls[i] = c;
 }
 
-// Exclusive scans of the four class bits over the points (one block), totals in tot[4].
-__global__ void __launch_bounds__(1024) k_densify_scan(int64_t n, const uint32_t* __restrict__ cls,
-                                                       uint32_t* __restrict__ pos, uint32_t* __restrict__ tot) {
-  __shared__ uint32_t sh[4][32];
+// Exclusive scans of the four class bits over the points, in three launches: per-block
+// counts (1024 points per block), a scan of the block counts (one block; totals in
+// tot[4]), then each block's exclusive scan offset by its block prefix.
+constexpr int kDensScanBlock = 1024;
+
+__device__ __forceinline__ void block_scan4(uint32_t c, uint32_t (*sh)[32], uint32_t (&excl)[4], uint32_t (&all)[4]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
-  uint32_t carry[4] = {0, 0, 0, 0};
-  for (int64_t base = 0; base < n; base += blockDim.x) {
-    const int64_t i = base + threadIdx.x;
-    const uint32_t c = i < n ? cls[i] : 0u;
-    uint32_t x[4];
+  uint32_t x[4];
 #pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const uint32_t f = (c >> b) & 1u;
-      uint32_t s = f;
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-        if (lane >= o) s += y;
-      }
-      if (lane == 31) sh[b][warp] = s;
-      x[b] = s - f;  // exclusive within the warp
+  for (int b = 0; b < 4; ++b) {
+    const uint32_t f = (c >> b) & 1u;
+    uint32_t s = f;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
     }
+    if (lane == 31) sh[b][warp] = s;
+    x[b] = s - f;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < nw; ++w) {
+      const uint32_t t = sh[b][w];
+      if (w < warp) before += t;
+      total += t;
+    }
+    excl[b] = before + x[b];
+    all[b] = total;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kDensScanBlock) k_densify_block_counts(int64_t n, const uint32_t* __restrict__ cls,
+                                                                       uint32_t* __restrict__ bcount) {
+  __shared__ uint32_t sh[4][32];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t excl[4], all[4];
+  block_scan4(i < n ? cls[i] : 0u, sh, excl, all);
+  if (threadIdx.x < 4) bcount[4 * (size_t)blockIdx.x + threadIdx.x] = all[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(1024) k_densify_block_prefix(int nblocks, uint32_t* __restrict__ bcount,
+                                                               uint32_t* __restrict__ tot) {
+  __shared__ uint32_t sh[4 * 32];  // per warp (32) and column (4)
+  const int b = threadIdx.x & 3;  // four columns, 256 threads each
+  const int lane = threadIdx.x & 31;
+  // column b, strided by 4: thread handles blocks j = (threadIdx.x >> 2) + 256 k
+  uint32_t carry = 0;
+  for (int base = 0; base < nblocks; base += 256) {
+    const int j = base + (threadIdx.x >> 2);
+    const uint32_t v = j < nblocks ? bcount[4 * (size_t)j + b] : 0u;
+    // inclusive scan over j within the column: lanes of a warp hold 8 consecutive j of
+    // each of the 4 columns (lane = 4 * jj + b)
+    uint32_t x = v;
+    for (int o = 4; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const int warp = threadIdx.x >> 5;
+    if (lane >= 28) sh[4 * warp + (lane - 28)] = x;  // warp totals per column
     __syncthreads();
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      uint32_t before = 0, all = 0;
-      for (int w = 0; w < nw; ++w) {
-        const uint32_t t = sh[b][w];
-        if (w < warp) before += t;
-        all += t;
-      }
-      if (i < n) pos[4 * i + b] = carry[b] + before + x[b];
-      carry[b] += all;
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < 32; ++w) {
+      const uint32_t t = sh[4 * w + b];
+      if (w < warp) before += t;
+      total += t;
     }
+    if (j < nblocks) bcount[4 * (size_t)j + b] = carry + before + x - v;
+    carry += total;
     __syncthreads();
   }
-  if (threadIdx.x == 0)
-    for (int b = 0; b < 4; ++b) tot[b] = carry[b];
+  if (threadIdx.x < 4) tot[b] = carry;
+}
+
+__global__ void __launch_bounds__(kDensScanBlock) k_densify_positions(int64_t n, const uint32_t* __restrict__ cls,
+                                                                    const uint32_t* __restrict__ bprefix,
+                                                                    uint32_t* __restrict__ pos) {
+  __shared__ uint32_t sh[4][32];
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t excl[4], all[4];
+  block_scan4(i < n ? cls[i] : 0u, sh, excl, all);
+  if (i < n) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) pos[4 * i + b] = bprefix[4 * (size_t)blockIdx.x + b] + excl[b];
+  }
 }
 
 // out_src[r] = source point of output row r, out_kind[r] = 0 original, 1 clone,
@@ -253,7 +332,8 @@ extern "C" int cfgs_gaussian_adam(int32_t num_groups, float* const* params, cons
     a.m[k] = exp_avg[k];
     a.v[k] = exp_avg_sq[k];
     a.begin[k] = off;
-    off += numel[k];
+    a.numel[k] = numel[k];
+    off += (numel[k] + 3) / 4;
     a.step_size[k] = (float)(-(lr[k] / bc1));
     a.bc2_sqrt[k] = (float)std::sqrt(bc2);
     a.eps[k] = (float)eps;
@@ -279,8 +359,10 @@ extern "C" int cfgs_densify_stats(int64_t num_gaussians, const int32_t* radii, c
 extern "C" size_t cfgs_densify_workspace_bytes(int64_t num_gaussians) {
   if (num_gaussians < 0) return 0;
   const size_t n = (size_t)(num_gaussians > 0 ? num_gaussians : 1);
+  const size_t nb = (n + kDensScanBlock - 1) / kDensScanBlock;
   return align256(sizeof(uint32_t) * n) + align256(sizeof(uint32_t) * 4 * n) + align256(sizeof(uint32_t) * 4) +
-         align256(sizeof(uint32_t) * 3 * n) + align256(sizeof(uint32_t) * 3 * n) + align256(3 * n);
+         align256(sizeof(uint32_t) * 3 * n) + align256(sizeof(uint32_t) * 3 * n) + align256(3 * n) +
+         align256(sizeof(uint32_t) * 4 * nb);
 }
 
 extern "C" int cfgs_densify_plan(int64_t num_gaussians, const float* grad_accum, const float* denom,
@@ -297,9 +379,22 @@ extern "C" int cfgs_densify_plan(int64_t num_gaussians, const float* grad_accum,
   uint32_t* cls = reinterpret_cast<uint32_t*>(w);
   uint32_t* pos = reinterpret_cast<uint32_t*>(w + align256(sizeof(uint32_t) * n));
   uint32_t* tot = reinterpret_cast<uint32_t*>(w + align256(sizeof(uint32_t) * n) + align256(sizeof(uint32_t) * 4 * n));
+  const size_t o_src = align256(sizeof(uint32_t) * n) + align256(sizeof(uint32_t) * 4 * n) +
+                       align256(sizeof(uint32_t) * 4);
+  const size_t o_rank = o_src + align256(sizeof(uint32_t) * 3 * n);
+  const size_t o_kind = o_rank + align256(sizeof(uint32_t) * 3 * n);
+  const size_t o_bcount = o_kind + align256(3 * (size_t)n);
+  uint32_t* src = reinterpret_cast<uint32_t*>(w + o_src);
+  uint32_t* rank = reinterpret_cast<uint32_t*>(w + o_rank);
+  uint8_t* kind = reinterpret_cast<uint8_t*>(w + o_kind);
+  uint32_t* bcount = reinterpret_cast<uint32_t*>(w + o_bcount);
+  const int nb = div_up(n, kDensScanBlock);
   DensifyParams d{max_grad, min_opacity, extent, percent_dense, prune_big};
   k_densify_classify<<<div_up(n, 256), 256, 0, st>>>(n, grad_accum, denom, scaling, opacity, d, cls);
-  k_densify_scan<<<1, 1024, 0, st>>>(n, cls, pos, tot);
+  k_densify_block_counts<<<nb, kDensScanBlock, 0, st>>>(n, cls, bcount);
+  k_densify_block_prefix<<<1, 1024, 0, st>>>(nb, bcount, tot);
+  k_densify_positions<<<nb, kDensScanBlock, 0, st>>>(n, cls, bcount, pos);
+  k_densify_map<<<div_up(n, 256), 256, 0, st>>>(n, cls, pos, tot, src, kind, rank);
   uint32_t h[4];
   if (cudaMemcpyAsync(h, tot, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
@@ -309,8 +404,8 @@ extern "C" int cfgs_densify_plan(int64_t num_gaussians, const float* grad_accum,
   return CFGS_OK;
 }
 
-// Builds the output row map for the plan in `workspace` (after cfgs_densify_plan) and
-// writes one parameter array: rows = counts[0] + counts[1] + 2 counts[3].
+// Writes one parameter array of the new model from the row map cfgs_densify_plan left in
+// `workspace`: rows = counts[0] + counts[1] + 2 counts[3].
 // role 0: plain parameter (copied), 1: Adam moment (zero for new rows), 2: xyz, 3: scaling
 // (children computed), z = standard-normal draws [2][counts[2]][3] for roles 2 and 3.
 extern "C" int cfgs_densify_write(int64_t num_gaussians, void* workspace, const int64_t counts[4], int32_t width,
@@ -328,16 +423,11 @@ extern "C" int cfgs_densify_write(int64_t num_gaussians, void* workspace, const 
   const size_t o_src = o_tot + align256(sizeof(uint32_t) * 4);
   const size_t o_rank = o_src + align256(sizeof(uint32_t) * 3 * n);
   const size_t o_kind = o_rank + align256(sizeof(uint32_t) * 3 * n);
-  uint32_t* cls = reinterpret_cast<uint32_t*>(w);
-  uint32_t* pos = reinterpret_cast<uint32_t*>(w + o_pos);
-  uint32_t* tot = reinterpret_cast<uint32_t*>(w + o_tot);
   uint32_t* src = reinterpret_cast<uint32_t*>(w + o_src);
   uint32_t* rank = reinterpret_cast<uint32_t*>(w + o_rank);
   uint8_t* kind = reinterpret_cast<uint8_t*>(w + o_kind);
   const int64_t rows = counts[0] + counts[1] + 2 * counts[3];
   if (rows > 3 * n) return CFGS_ERR_INVALID_ARGUMENT;
-  // the row map is rebuilt per call (cheap; keeps the calls independent)
-  k_densify_map<<<div_up(n, 256), 256, 0, st>>>(n, cls, pos, tot, src, kind, rank);
   if (rows > 0) {
     k_densify_gather<<<div_up(rows * width, 256), 256, 0, st>>>(rows, width, in, out, src, kind, role == 1);
     if (role >= 2 && counts[3] > 0)
