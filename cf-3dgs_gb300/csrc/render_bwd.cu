@@ -239,6 +239,8 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
   __syncthreads();
   const uint32_t my_last = max(p0.last, p1.last);
   if (my_last) atomicMax(&s_max, my_last);
+  // instances at or past the warp's largest contributor count reach none of its pixels
+  const int warp_last = (int)__reduce_max_sync(0xffffffffu, my_last);
   __syncthreads();
   const int max_last = (int)s_max;
 
@@ -263,7 +265,7 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
     for (int r = 0; r < kBwdBatch / 32; ++r) {
       const int j = r * 32 + lane;
       bool k = false;
-      if (j < cnt) {
+      if (j < cnt && base + j < warp_last) {
         const float4 xyt = s_xyt[j];
         const float4 co = s_co[j];
         k = box_may_contribute(make_float2(xyt.x, xyt.y), co.x, co.y, co.z, xyt.z, bxf0, bxf1, byf0, byf1);
