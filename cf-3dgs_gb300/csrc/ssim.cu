@@ -12,9 +12,10 @@
 // and the backward forms dL/dx_q = g (W*a + 2 x_q W*b + y_q W*c)_q with g = dL/dmean
 // (the window is symmetric, so the transposed convolution is the same convolution).
 //
-// Both kernels work on 32x16 output tiles of one channel: the tile and a 5-pixel halo
-// are staged in shared memory (zero outside the image), a horizontal 11-tap pass runs
-// over all staged rows, then a vertical 11-tap pass per output pixel.
+// Both kernels work on 32x32 output tiles of one channel: the tile and a 5-pixel halo
+// are staged in shared memory (zero outside the image); a horizontal 11-tap pass over all
+// staged rows and then a vertical pass compute runs of 4 outputs per thread, each input
+// loaded once per run and the window slid in registers.
 #include <cmath>
 
 #include "cfgs_internal.cuh"
@@ -23,8 +24,11 @@ namespace cfgs {
 
 constexpr int kSsimR = 5;  // window radius
 constexpr int kSsimTaps = 2 * kSsimR + 1;
-constexpr int kSsimTW = 32, kSsimTH = 16;
-constexpr int kSsimSW = kSsimTW + 2 * kSsimR, kSsimSH = kSsimTH + 2 * kSsimR;  // staged tile
+constexpr int kSsimT = 32;                        // output tile: 32 x 32
+constexpr int kSsimS = kSsimT + 2 * kSsimR;       // staged rows / columns (42)
+constexpr int kSsimSP = kSsimS + 1;               // staged row stride (43: conflict-free)
+constexpr int kSsimHP = kSsimT + 1;               // horizontal-result row stride (33)
+constexpr int kSsimRun = 4;                       // outputs per thread along a row / column
 constexpr int kSsimThreads = 256;
 constexpr float kSsimC1 = 0.0001f, kSsimC2 = 0.0009f;
 
@@ -51,68 +55,101 @@ __device__ __forceinline__ double block_sum_fixed(double v, double* sh) {
   return t;  // valid in thread 0
 }
 
+// Horizontal 11-tap sums of NQ staged quantities for kSsimRun consecutive outputs of one
+// staged row: the 14 inputs are loaded once and the window slides in registers.
+// prod(u, v, out) expands two staged values into the NQ quantities.
+template <int NQ, class Prod>
+__device__ __forceinline__ void hpass_run(const float* a_row, const float* b_row, int c0, float (&out)[NQ][kSsimRun],
+                                          Prod prod) {
+  float q[kSsimRun + 2 * kSsimR][NQ];
+#pragma unroll
+  for (int k = 0; k < kSsimRun + 2 * kSsimR; ++k) prod(a_row[c0 + k], b_row ? b_row[c0 + k] : 0.f, q[k]);
+#pragma unroll
+  for (int u = 0; u < kSsimRun; ++u)
+#pragma unroll
+    for (int n = 0; n < NQ; ++n) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k < kSsimTaps; ++k) acc = fmaf(c_ssim_w[k], q[u + k][n], acc);
+      out[n][u] = acc;
+    }
+}
+
 __global__ void __launch_bounds__(kSsimThreads) k_ssim_fwd(SsimDims d, const float* __restrict__ img1,
                                                            const float* __restrict__ img2, float* __restrict__ maps,
                                                            double* __restrict__ partials, float inv_count) {
-  __shared__ float s_x[kSsimSH][kSsimSW], s_y[kSsimSH][kSsimSW];
-  __shared__ float s_h[5][kSsimSH][kSsimTW];  // horizontal sums of x, y, xx, yy, xy
+  __shared__ float s_x[kSsimS * kSsimSP], s_y[kSsimS * kSsimSP];
+  __shared__ float s_h[5][kSsimS * kSsimHP];  // horizontal sums of x, y, xx, yy, xy
   __shared__ double s_red[kSsimThreads / 32];
   const int tile = blockIdx.x, ch = blockIdx.y;
-  const int x0 = (tile % d.tiles_x) * kSsimTW, y0 = (tile / d.tiles_x) * kSsimTH;
+  const int x0 = (tile % d.tiles_x) * kSsimT, y0 = (tile / d.tiles_x) * kSsimT;
   const size_t plane = (size_t)d.H * d.W;
   const float* X = img1 + ch * plane;
   const float* Y = img2 + ch * plane;
-  for (int i = threadIdx.x; i < kSsimSH * kSsimSW; i += kSsimThreads) {
-    const int r = i / kSsimSW, c = i % kSsimSW;
-    s_x[r][c] = load_or_zero(X, d.H, d.W, y0 + r - kSsimR, x0 + c - kSsimR);
-    s_y[r][c] = load_or_zero(Y, d.H, d.W, y0 + r - kSsimR, x0 + c - kSsimR);
+  for (int i = threadIdx.x; i < kSsimS * kSsimS; i += kSsimThreads) {
+    const int r = i / kSsimS, c = i % kSsimS;
+    s_x[r * kSsimSP + c] = load_or_zero(X, d.H, d.W, y0 + r - kSsimR, x0 + c - kSsimR);
+    s_y[r * kSsimSP + c] = load_or_zero(Y, d.H, d.W, y0 + r - kSsimR, x0 + c - kSsimR);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < kSsimSH * kSsimTW; i += kSsimThreads) {
-    const int r = i / kSsimTW, c = i % kSsimTW;
-    float hx = 0.f, hy = 0.f, hxx = 0.f, hyy = 0.f, hxy = 0.f;
+  // horizontal: item = (staged row r, run of 4 output columns)
+  for (int it = threadIdx.x; it < kSsimS * (kSsimT / kSsimRun); it += kSsimThreads) {
+    const int r = it / (kSsimT / kSsimRun), c0 = (it % (kSsimT / kSsimRun)) * kSsimRun;
+    float out[5][kSsimRun];
+    hpass_run<5>(s_x + r * kSsimSP, s_y + r * kSsimSP, c0, out, [](float u, float v, float (&q)[5]) {
+      q[0] = u;
+      q[1] = v;
+      q[2] = u * u;
+      q[3] = v * v;
+      q[4] = u * v;
+    });
 #pragma unroll
-    for (int k = 0; k < kSsimTaps; ++k) {
-      const float w = c_ssim_w[k], u = s_x[r][c + k], v = s_y[r][c + k];
-      hx = fmaf(w, u, hx);
-      hy = fmaf(w, v, hy);
-      hxx = fmaf(w, u * u, hxx);
-      hyy = fmaf(w, v * v, hyy);
-      hxy = fmaf(w, u * v, hxy);
-    }
-    s_h[0][r][c] = hx;
-    s_h[1][r][c] = hy;
-    s_h[2][r][c] = hxx;
-    s_h[3][r][c] = hyy;
-    s_h[4][r][c] = hxy;
+    for (int n = 0; n < 5; ++n)
+#pragma unroll
+      for (int u = 0; u < kSsimRun; ++u) s_h[n][r * kSsimHP + c0 + u] = out[n][u];
   }
   __syncthreads();
+  // vertical: item = (output column c, run of 4 output rows); one item per thread
   double ssum = 0.0;
-  for (int i = threadIdx.x; i < kSsimTH * kSsimTW; i += kSsimThreads) {
-    const int r = i / kSsimTW, c = i % kSsimTW;
-    const int py = y0 + r, px = x0 + c;
-    if (py >= d.H || px >= d.W) continue;
-    float mu1 = 0.f, mu2 = 0.f, exx = 0.f, eyy = 0.f, exy = 0.f;
+  {
+    const int c = threadIdx.x % kSsimT, r0 = (threadIdx.x / kSsimT) * kSsimRun;
+    float acc[5][kSsimRun];
 #pragma unroll
-    for (int k = 0; k < kSsimTaps; ++k) {
-      const float w = c_ssim_w[k];
-      mu1 = fmaf(w, s_h[0][r + k][c], mu1);
-      mu2 = fmaf(w, s_h[1][r + k][c], mu2);
-      exx = fmaf(w, s_h[2][r + k][c], exx);
-      eyy = fmaf(w, s_h[3][r + k][c], eyy);
-      exy = fmaf(w, s_h[4][r + k][c], exy);
+    for (int n = 0; n < 5; ++n)
+#pragma unroll
+      for (int u = 0; u < kSsimRun; ++u) acc[n][u] = 0.f;
+#pragma unroll
+    for (int k = 0; k < kSsimRun + 2 * kSsimR; ++k) {
+      float v[5];
+#pragma unroll
+      for (int n = 0; n < 5; ++n) v[n] = s_h[n][(r0 + k) * kSsimHP + c];
+#pragma unroll
+      for (int u = 0; u < kSsimRun; ++u) {
+        const int tap = k - u;
+        if (tap >= 0 && tap < kSsimTaps) {
+#pragma unroll
+          for (int n = 0; n < 5; ++n) acc[n][u] = fmaf(c_ssim_w[tap], v[n], acc[n][u]);
+        }
+      }
     }
-    const float m11 = mu1 * mu1, m22 = mu2 * mu2, m12 = mu1 * mu2;
-    const float A = 2.f * m12 + kSsimC1, B = 2.f * (exy - m12) + kSsimC2;
-    const float Cc = m11 + m22 + kSsimC1, D = (exx - m11) + (eyy - m22) + kSsimC2;
-    const float S = (A * B) / (Cc * D);
-    ssum += (double)S;
-    const size_t q = ch * plane + (size_t)py * d.W + px;
-    // dS/dmu1 = S (2 mu2/A - 2 mu2/B - 2 mu1/C + 2 mu1/D); dS/dexx = -S/D; dS/dexy = 2 S/B
-    const float da = S * (2.f * mu2 * (1.f / A - 1.f / B) + 2.f * mu1 * (1.f / D - 1.f / Cc));
-    maps[q] = inv_count * da;
-    maps[(size_t)d.C * plane + q] = inv_count * (-S / D);
-    maps[2 * (size_t)d.C * plane + q] = inv_count * (2.f * S / B);
+    const int px = x0 + c;
+#pragma unroll
+    for (int u = 0; u < kSsimRun; ++u) {
+      const int py = y0 + r0 + u;
+      if (py >= d.H || px >= d.W) continue;
+      const float mu1 = acc[0][u], mu2 = acc[1][u], exx = acc[2][u], eyy = acc[3][u], exy = acc[4][u];
+      const float m11 = mu1 * mu1, m22 = mu2 * mu2, m12 = mu1 * mu2;
+      const float A = 2.f * m12 + kSsimC1, B = 2.f * (exy - m12) + kSsimC2;
+      const float Cc = m11 + m22 + kSsimC1, D = (exx - m11) + (eyy - m22) + kSsimC2;
+      const float S = (A * B) / (Cc * D);
+      ssum += (double)S;
+      const size_t q = ch * plane + (size_t)py * d.W + px;
+      // dS/dmu1 = S (2 mu2/A - 2 mu2/B - 2 mu1/C + 2 mu1/D); dS/dexx = -S/D; dS/dexy = 2 S/B
+      const float da = S * (2.f * mu2 * (1.f / A - 1.f / B) + 2.f * mu1 * (1.f / D - 1.f / Cc));
+      maps[q] = inv_count * da;
+      maps[(size_t)d.C * plane + q] = inv_count * (-S / D);
+      maps[2 * (size_t)d.C * plane + q] = inv_count * (2.f * S / B);
+    }
   }
   const double t = block_sum_fixed(ssum, s_red);
   if (threadIdx.x == 0) partials[(size_t)ch * gridDim.x + tile] = t;
@@ -133,49 +170,58 @@ __global__ void __launch_bounds__(kSsimThreads) k_ssim_bwd(SsimDims d, const flo
                                                            const float* __restrict__ maps,
                                                            const float* __restrict__ dL_dmean,
                                                            float* __restrict__ dL_dimg1) {
-  __shared__ float s_m[3][kSsimSH][kSsimSW];
-  __shared__ float s_h[3][kSsimSH][kSsimTW];
+  __shared__ float s_m[3][kSsimS * kSsimSP];
+  __shared__ float s_h[3][kSsimS * kSsimHP];
   const int tile = blockIdx.x, ch = blockIdx.y;
-  const int x0 = (tile % d.tiles_x) * kSsimTW, y0 = (tile / d.tiles_x) * kSsimTH;
+  const int x0 = (tile % d.tiles_x) * kSsimT, y0 = (tile / d.tiles_x) * kSsimT;
   const size_t plane = (size_t)d.H * d.W;
-  for (int i = threadIdx.x; i < kSsimSH * kSsimSW; i += kSsimThreads) {
-    const int r = i / kSsimSW, c = i % kSsimSW;
+  for (int i = threadIdx.x; i < kSsimS * kSsimS; i += kSsimThreads) {
+    const int r = i / kSsimS, c = i % kSsimS;
 #pragma unroll
     for (int m = 0; m < 3; ++m)
-      s_m[m][r][c] =
+      s_m[m][r * kSsimSP + c] =
           load_or_zero(maps + ((size_t)m * d.C + ch) * plane, d.H, d.W, y0 + r - kSsimR, x0 + c - kSsimR);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < kSsimSH * kSsimTW; i += kSsimThreads) {
-    const int r = i / kSsimTW, c = i % kSsimTW;
-    float h0 = 0.f, h1 = 0.f, h2 = 0.f;
+  for (int it = threadIdx.x; it < kSsimS * (kSsimT / kSsimRun); it += kSsimThreads) {
+    const int r = it / (kSsimT / kSsimRun), c0 = (it % (kSsimT / kSsimRun)) * kSsimRun;
 #pragma unroll
-    for (int k = 0; k < kSsimTaps; ++k) {
-      const float w = c_ssim_w[k];
-      h0 = fmaf(w, s_m[0][r][c + k], h0);
-      h1 = fmaf(w, s_m[1][r][c + k], h1);
-      h2 = fmaf(w, s_m[2][r][c + k], h2);
+    for (int m = 0; m < 3; ++m) {
+      float out[1][kSsimRun];
+      hpass_run<1>(s_m[m] + r * kSsimSP, nullptr, c0, out, [](float u, float, float (&q)[1]) { q[0] = u; });
+#pragma unroll
+      for (int u = 0; u < kSsimRun; ++u) s_h[m][r * kSsimHP + c0 + u] = out[0][u];
     }
-    s_h[0][r][c] = h0;
-    s_h[1][r][c] = h1;
-    s_h[2][r][c] = h2;
   }
   __syncthreads();
   const float g = *dL_dmean;
-  for (int i = threadIdx.x; i < kSsimTH * kSsimTW; i += kSsimThreads) {
-    const int r = i / kSsimTW, c = i % kSsimTW;
-    const int py = y0 + r, px = x0 + c;
-    if (py >= d.H || px >= d.W) continue;
-    float va = 0.f, vb = 0.f, vc = 0.f;
+  const int c = threadIdx.x % kSsimT, r0 = (threadIdx.x / kSsimT) * kSsimRun;
+  float acc[3][kSsimRun];
 #pragma unroll
-    for (int k = 0; k < kSsimTaps; ++k) {
-      const float w = c_ssim_w[k];
-      va = fmaf(w, s_h[0][r + k][c], va);
-      vb = fmaf(w, s_h[1][r + k][c], vb);
-      vc = fmaf(w, s_h[2][r + k][c], vc);
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int u = 0; u < kSsimRun; ++u) acc[m][u] = 0.f;
+#pragma unroll
+  for (int k = 0; k < kSsimRun + 2 * kSsimR; ++k) {
+    float v[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) v[m] = s_h[m][(r0 + k) * kSsimHP + c];
+#pragma unroll
+    for (int u = 0; u < kSsimRun; ++u) {
+      const int tap = k - u;
+      if (tap >= 0 && tap < kSsimTaps) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) acc[m][u] = fmaf(c_ssim_w[tap], v[m], acc[m][u]);
+      }
     }
+  }
+  const int px = x0 + c;
+#pragma unroll
+  for (int u = 0; u < kSsimRun; ++u) {
+    const int py = y0 + r0 + u;
+    if (py >= d.H || px >= d.W) continue;
     const size_t q = ch * plane + (size_t)py * d.W + px;
-    dL_dimg1[q] = g * (va + 2.f * img1[q] * vb + img2[q] * vc);
+    dL_dimg1[q] = g * (acc[0][u] + 2.f * img1[q] * acc[1][u] + img2[q] * acc[2][u]);
   }
 }
 
@@ -208,8 +254,8 @@ SsimDims dims(int32_t C, int32_t H, int32_t W) {
   d.C = C;
   d.H = H;
   d.W = W;
-  d.tiles_x = (W + kSsimTW - 1) / kSsimTW;
-  d.tiles_y = (H + kSsimTH - 1) / kSsimTH;
+  d.tiles_x = (W + kSsimT - 1) / kSsimT;
+  d.tiles_y = (H + kSsimT - 1) / kSsimT;
   return d;
 }
 
