@@ -34,6 +34,13 @@ constexpr float kSsimC1 = 0.0001f, kSsimC2 = 0.0009f;
 
 __constant__ float c_ssim_w[kSsimTaps];
 
+// Reciprocal to within one unit in the last place (the loss is held to a tolerance).
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 struct SsimDims {
   int C, H, W, tiles_x, tiles_y;
 };
@@ -110,7 +117,7 @@ __global__ void __launch_bounds__(kSsimThreads) k_ssim_fwd(SsimDims d, const flo
   }
   __syncthreads();
   // vertical: item = (output column c, run of 4 output rows); one item per thread
-  double ssum = 0.0;
+  float ssum = 0.f;
   {
     const int c = threadIdx.x % kSsimT, r0 = (threadIdx.x / kSsimT) * kSsimRun;
     float acc[5][kSsimRun];
@@ -141,17 +148,18 @@ __global__ void __launch_bounds__(kSsimThreads) k_ssim_fwd(SsimDims d, const flo
       const float m11 = mu1 * mu1, m22 = mu2 * mu2, m12 = mu1 * mu2;
       const float A = 2.f * m12 + kSsimC1, B = 2.f * (exy - m12) + kSsimC2;
       const float Cc = m11 + m22 + kSsimC1, D = (exx - m11) + (eyy - m22) + kSsimC2;
-      const float S = (A * B) / (Cc * D);
-      ssum += (double)S;
+      const float rA = rcp_approx(A), rB = rcp_approx(B), rC = rcp_approx(Cc), rD = rcp_approx(D);
+      const float S = (A * B) * (rC * rD);
+      ssum += S;
       const size_t q = ch * plane + (size_t)py * d.W + px;
       // dS/dmu1 = S (2 mu2/A - 2 mu2/B - 2 mu1/C + 2 mu1/D); dS/dexx = -S/D; dS/dexy = 2 S/B
-      const float da = S * (2.f * mu2 * (1.f / A - 1.f / B) + 2.f * mu1 * (1.f / D - 1.f / Cc));
+      const float da = S * (2.f * mu2 * (rA - rB) + 2.f * mu1 * (rD - rC));
       maps[q] = inv_count * da;
-      maps[(size_t)d.C * plane + q] = inv_count * (-S / D);
-      maps[2 * (size_t)d.C * plane + q] = inv_count * (2.f * S / B);
+      maps[(size_t)d.C * plane + q] = inv_count * (-S * rD);
+      maps[2 * (size_t)d.C * plane + q] = inv_count * (2.f * S * rB);
     }
   }
-  const double t = block_sum_fixed(ssum, s_red);
+  const double t = block_sum_fixed((double)ssum, s_red);
   if (threadIdx.x == 0) partials[(size_t)ch * gridDim.x + tile] = t;
 }
 
