@@ -407,6 +407,30 @@ __device__ __forceinline__ float2 exp_ref_inrange2(float2 x) {
   return mul2(p, sc);
 }
 
+// ---------------------------------------------------------------------------
+// mbarrier helpers for bulk and tensor copies into shared memory.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Bounded wait for phase `parity` of an mbarrier; false if it did not complete.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 22); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
 // Lower bound on the exponent of a Gaussian of opacity o that can still give
 // alpha >= 1/255: below it, min(0.99, o exp_ref(power)) < 1/255 for certain, so the
 // pixel can skip the exponential without changing any output. The bound sits 1e-3

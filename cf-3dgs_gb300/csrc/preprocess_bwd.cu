@@ -361,22 +361,6 @@ __device__ __forceinline__ void zero_gradients(const PreBwdArgs<Scenes>& a, int6
     for (int k = 0; k < 3 * M; ++k) dsh_dst[k] = 0.f;
 }
 
-__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Bounded wait for phase `parity` of an mbarrier; false if it did not complete.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 22); ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
-}
-
 // Full form: all eight gradient arrays. Pose-only form (pose_partials set): only
 // dL/dmean (through projection, covariance and SH view direction) is formed and the
 // block's SE(3) gradient terms — sum g and sum (R p) x g in float64 with the scene's
@@ -402,8 +386,7 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
   const uint32_t bar = smem_addr(&s_bar);
   if (bulk) {
     if (threadIdx.x == 0) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      mbar_init(bar, 1);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
