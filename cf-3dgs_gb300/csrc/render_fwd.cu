@@ -12,7 +12,7 @@ namespace cfgs {
 
 constexpr int kRenderThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
 constexpr int kRenderBatch = 128;
-static_assert(kRenderBatch <= kRenderThreads && kRenderBatch % 32 == 0, "one staged instance per thread at most");
+static_assert(kRenderBatch % kRenderThreads == 0 && kRenderBatch % 32 == 0, "whole staging rounds");
 
 // Front-to-back state of a lane's two pixels (.x: row r, .y: row r + 4) and one
 // compositing step of both: the published loop body per pixel, with the exponential
@@ -69,8 +69,8 @@ __device__ __forceinline__ void composite_pair(PairFwd& p, float pxf, float2 pyf
 
 // One block of 128 threads per 16x16 tile; warp w covers the 8x8 pixel box
 // (8 (w & 1), 8 (w >> 1)) and each lane two pixels of it, rows r and r + 4. Batches of
-// kRenderBatch instances are gathered into shared memory, one per thread of the first
-// kRenderBatch threads (per-Gaussian data stays L2-resident).
+// kRenderBatch instances are gathered into shared memory, kRenderBatch / kRenderThreads
+// per thread (per-Gaussian data stays L2-resident).
 // Two exact shortcuts skip work whose outcome is known: each warp keeps only the
 // instances whose alpha >= 1/255 ellipse can reach its box (box_may_contribute, one test
 // per instance and warp), and a pixel skips the exponential when the exponent lies
@@ -100,14 +100,18 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes
   const float2 pyf = make_float2(pyf0, pyf1);
   for (int base = 0; base < n; base += kRenderBatch) {
     if (__syncthreads_count(pp.done0 && pp.done1) == kRenderThreads) break;
-    int i = base + threadIdx.x;
-    if ((int)threadIdx.x < kRenderBatch && i < n) {
-      uint32_t g = a.sorted_gid[lo + i];
-      float2 m = a.xy[g];
-      float4 co = a.conic_op[g];
-      s_xyt[threadIdx.x] = make_float4(m.x, m.y, alpha_threshold(co.w), 0.0f);
-      s_co[threadIdx.x] = make_float4(-0.5f * co.x, -co.y, -0.5f * co.z, co.w);
-      s_rgbd[threadIdx.x] = a.rgbd[g];
+#pragma unroll
+    for (int k = 0; k < kRenderBatch / kRenderThreads; ++k) {
+      const int j = k * kRenderThreads + threadIdx.x;
+      const int i = base + j;
+      if (i < n) {
+        uint32_t g = a.sorted_gid[lo + i];
+        float2 m = a.xy[g];
+        float4 co = a.conic_op[g];
+        s_xyt[j] = make_float4(m.x, m.y, alpha_threshold(co.w), 0.0f);
+        s_co[j] = make_float4(-0.5f * co.x, -co.y, -0.5f * co.z, co.w);
+        s_rgbd[j] = a.rgbd[g];
+      }
     }
     __syncthreads();
     const int cnt = min(kRenderBatch, n - base);
