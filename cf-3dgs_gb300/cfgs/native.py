@@ -141,6 +141,9 @@ EXPORTS = {
     "cfgs_ssim_scratch_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     "cfgs_ssim_forward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_ssim_backward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "cfgs_l1_loss_scratch_bytes": (C.c_size_t, [C.c_int64]),
+    "cfgs_l1_loss_forward": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, _vp, _vp]),
+    "cfgs_l1_loss_backward": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, _vp]),
     "cfgs_batch_plan": (C.c_int, [C.c_int32, C.POINTER(BatchScene), _vp, C.POINTER(BatchPlan), _vp, _vp, _vp, _vp,
                                   _vp, _vp]),
     "cfgs_batch_init": (C.c_int, [C.POINTER(BatchArgs), _vp]),

@@ -246,8 +246,12 @@ def render(prob: PoseProblem, means: torch.Tensor, cov6: torch.Tensor | None = N
     return color
 
 
-def l1(img: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
-    """RGB L1 of the clamped render (trainer/losses.py:98-136 with lambda_dssim = 0)."""
+def l1(img: torch.Tensor, target: torch.Tensor, fused: bool = False) -> torch.Tensor:
+    """RGB L1 of the clamped render (trainer/losses.py:98-136 with lambda_dssim = 0):
+    PyTorch operations on the plain path, the fused L1 kernels on the fused path."""
+    if fused:
+        from .loss import l1_loss
+        return l1_loss(img, target, clamp=True)
     return (img.clamp(0, 1) - target).abs().mean()
 
 
@@ -272,14 +276,12 @@ def photometric_loss(img: torch.Tensor, target: torch.Tensor, lambda_dssim: floa
     """(1 - lambda) L1 + lambda (1 - SSIM) of the clamped render (trainer/losses.py:98-136;
     CF-3DGS uses lambda_dssim = 0.2). lambda 0 is the RGB L1 alone."""
     if lambda_dssim == 0.0:
-        return l1(img, target)
+        return l1(img, target, fused)
     c = img.clamp(0, 1)
     if fused:
         from .ssim import ssim
-        s = ssim(c, target)
-    else:
-        s = ssim_torch(c, target)
-    return (1.0 - lambda_dssim) * (c - target).abs().mean() + lambda_dssim * (1.0 - s)
+        return (1.0 - lambda_dssim) * l1(img, target, fused=True) + lambda_dssim * (1.0 - ssim(c, target))
+    return (1.0 - lambda_dssim) * (c - target).abs().mean() + lambda_dssim * (1.0 - ssim_torch(c, target))
 
 
 def solve(prob: PoseProblem, iters: int = 300, lr: float = 1e-3, mode: str = "fused", record: bool = False,

@@ -263,6 +263,21 @@ int cfgs_ssim_forward(int32_t channels, int32_t height, int32_t width, const flo
 int cfgs_ssim_backward(int32_t channels, int32_t height, int32_t width, const float* img1, const float* img2,
                        const void* scratch, const float* dL_dmean, float* dL_dimg1, void* stream);
 
+/* ---- L1 photometric loss ------------------------------------------------------------
+ * mean |x - target| over n floats (utils/loss_utils.py:15-16, trainer/losses.py:139-140),
+ * of clamp(x, 0, 1) when clamp != 0 (the pose solve clamps the render before its loss:
+ * scene/gaussian_model_cf.py:885). cfgs_l1_loss_forward writes the mean to loss (device
+ * float; NaN for n = 0, as torch's mean) using `scratch` (cfgs_l1_loss_scratch_bytes) for
+ * block partial sums (deterministic: fixed partition, float64 fold); when dL_dx is not
+ * NULL it also writes, in the same pass, the gradient of the mean for an upstream
+ * gradient of 1. cfgs_l1_loss_backward writes dL/dx = dL_dloss[0] * d mean / dx as
+ * autograd forms it: (g / n) sign(c - target), zero where the clamp cuts (x < 0, x > 1). */
+size_t cfgs_l1_loss_scratch_bytes(int64_t n);
+int cfgs_l1_loss_forward(int64_t n, const float* x, const float* target, int32_t clamp, void* scratch, float* loss,
+                         float* dL_dx, void* stream);
+int cfgs_l1_loss_backward(int64_t n, const float* x, const float* target, int32_t clamp, const float* dL_dloss,
+                          float* dL_dx, void* stream);
+
 /* ---- frame initialisation (local Gaussians before each pose solve) ---------------------
  * kornia depth_to_3d (normalize_points=False; trainer/trainer.py:491): [H,W] depth ->
  * [H*W,3] camera-space points ((u - cx)/fx * d, (v - cy)/fy * d, d), row-major pixels. */

@@ -106,3 +106,14 @@ def test_pointcloud_abi_host_checks():
     assert lib.cfgs_voxel_down_sample(10, None, None, 0.0, None, None, None, native.C.byref(m), None) == 1
     assert lib.cfgs_voxel_down_sample(0, None, None, 0.01, None, None, None, native.C.byref(m), None) == 0
     assert m.value == 0
+
+
+def test_l1_loss_abi_host_checks():
+    from cfgs import native
+    lib = native.load()
+    assert lib.cfgs_l1_loss_scratch_bytes(6_220_800) >= 4 * 152 * 4
+    assert lib.cfgs_l1_loss_forward(-1, None, None, 1, None, None, None, None) == 1
+    assert lib.cfgs_l1_loss_forward(10, None, None, 1, None, None, None, None) == 1
+    assert lib.cfgs_l1_loss_backward(-1, None, None, 0, None, None, None) == 1
+    assert lib.cfgs_l1_loss_backward(10, None, None, 0, None, None, None) == 1
+    assert lib.cfgs_l1_loss_backward(0, None, None, 0, None, None, None) == 0
