@@ -117,7 +117,8 @@ bool args_ok(const CfgsBatchArgs* a) {
 
 extern "C" int cfgs_batch_init(const CfgsBatchArgs* a, void* stream) {
   if (!args_ok(a)) return CFGS_ERR_INVALID_ARGUMENT;
-  launch_batch_pose_init(a->num_scenes, a->xi, static_cast<PoseState*>(a->pose_states), (cudaStream_t)stream);
+  launch_batch_pose_init(a->num_scenes, a->xi, a->adam_state, static_cast<PoseState*>(a->pose_states), a->beta1,
+                         a->beta2, (cudaStream_t)stream);
   CFGS_CHECK_LAUNCH(0, stream);
   return CFGS_OK;
 }

@@ -193,6 +193,9 @@ struct BinningView {
 struct PoseState {     // per-scene rigid motion applied to the means before projection
   double R64[9];       // rotation of exp(xi), float64 (pose-gradient terms)
   double t64[3];
+  double Jl[9];        // SO(3) left Jacobian of phi and the block Q(rho, phi) of the SE(3) one:
+  double Q[9];         // dL/dxi = [[Jl, Q], [0, Jl]]^T dL/d(left perturbation)
+  double bc1, bc2;     // Adam bias corrections 1 - beta^step of the step the solve takes next
   float R[9];          // the same, rounded to float (positions)
   float t[3];
 };

@@ -114,7 +114,8 @@ template <class Scenes>
 void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st);
 template <class Scenes>
 void launch_preprocess_bwd(const PreBwdArgs<Scenes>& a, int blocks, cudaStream_t st);
-void launch_batch_pose_init(int count, const float* xi, PoseState* states, cudaStream_t st);
+void launch_batch_pose_init(int count, const float* xi, const float* adam_state, PoseState* states, double b1,
+                            double b2, cudaStream_t st);
 void launch_batch_pose_update(int count, const SceneDesc* descs, const double* partials, float* xi,
                               float* adam_state, PoseState* states, const CfgsCounts* counts, int64_t cap, double lr,
                               double b1, double b2, double eps, cudaStream_t st);

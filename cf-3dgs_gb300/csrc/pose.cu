@@ -263,13 +263,17 @@ __global__ void __launch_bounds__(kPoseThreads) k_pose_grad(PoseGradArgs a) {
 //   m = lerp(m, g, 1 - b1);  v = v * b2;  v = addcmul(v, g, g, 1 - b2);
 //   denom = sqrt(v) / sqrt(1 - b2^t) + eps;  p = addcdiv(p, m, denom, -lr / (1 - b1^t))
 // with the hyper-parameters as float64 scalars rounded to float32 per use, as torch
-// passes them, so both optimisers take the same steps.
+// passes them, so both optimisers take the same steps. bc1 = 1 - b1^t and
+// bc2 = 1 - b2^t are float64, as torch forms them on the host.
 // state per solve: m[6], v[6], step, 3 unused floats.
-__device__ void adam_step6(float* xi, const float* grad, float* st, double lr, double b1, double b2, double eps) {
+__device__ __forceinline__ double bias_correction(double beta, const float* st) {
+  return 1.0 - pow(beta, (double)(st[12] + 1.0f));
+}
+
+__device__ void adam_step6_bc(float* xi, const float* grad, float* st, double lr, double b1, double b2, double eps,
+                              double bc1, double bc2) {
   const float step = st[12] + 1.0f;
   const float w1 = (float)(1.0 - b1), mul2 = (float)b2, w2 = (float)(1.0 - b2);
-  const double bc1 = 1.0 - pow(b1, (double)step);
-  const double bc2 = 1.0 - pow(b2, (double)step);
   const float step_size = (float)(-(lr / bc1));
   const float bc2_sqrt = (float)sqrt(bc2);
   const float eps_f = (float)eps;
@@ -289,6 +293,10 @@ __device__ void adam_step6(float* xi, const float* grad, float* st, double lr, d
   st[12] = step;
 }
 
+__device__ void adam_step6(float* xi, const float* grad, float* st, double lr, double b1, double b2, double eps) {
+  adam_step6_bc(xi, grad, st, lr, b1, b2, eps, bias_correction(b1, st), bias_correction(b2, st));
+}
+
 __global__ void k_pose_adam(int count, float* xi, const float* grad, float* state, double lr, double b1, double b2,
                             double eps) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -296,13 +304,16 @@ __global__ void k_pose_adam(int count, float* xi, const float* grad, float* stat
   adam_step6(xi + 6 * (size_t)s, grad + 6 * (size_t)s, state + 16 * (size_t)s, lr, b1, b2, eps);
 }
 
-__device__ void pose_state_from_xi(const float* xi, PoseState* ps) {
+// The parts of a solve's pose state that depend on xi, split so that two threads can
+// form them at once: exp(xi) with the left Jacobian, and the Q block.
+__device__ void pose_state_exp(const float* xi, PoseState* ps) {
   SE3d X;
   double Jl[9];
   se3_exp(xi, &X, Jl);
   for (int k = 0; k < 9; ++k) {
     ps->R64[k] = X.R[k];
     ps->R[k] = (float)X.R[k];
+    ps->Jl[k] = Jl[k];
   }
   for (int k = 0; k < 3; ++k) {
     ps->t64[k] = X.t[k];
@@ -310,20 +321,55 @@ __device__ void pose_state_from_xi(const float* xi, PoseState* ps) {
   }
 }
 
-__global__ void k_batch_pose_init(int count, const float* xi, PoseState* states) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < count) pose_state_from_xi(xi + 6 * (size_t)s, states + s);
+__device__ void pose_state_Q(const float* xi, PoseState* ps) {
+  const double rho[3] = {xi[0], xi[1], xi[2]};
+  const double phi[3] = {xi[3], xi[4], xi[5]};
+  se3_Q(rho, phi, ps->Q);
+}
+
+// pose_grad_from_sums with exp(xi), Jl and Q taken from the solve's state.
+__device__ void pose_grad_from_state(const PoseState& ps, const double* tot, float* grad_out) {
+  const double gr[3] = {tot[0], tot[1], tot[2]};
+  double gp[3];
+  gp[0] = tot[3] + (ps.t64[1] * gr[2] - ps.t64[2] * gr[1]) + tot[6];
+  gp[1] = tot[4] + (ps.t64[2] * gr[0] - ps.t64[0] * gr[2]) + tot[7];
+  gp[2] = tot[5] + (ps.t64[0] * gr[1] - ps.t64[1] * gr[0]) + tot[8];
+  const double* Jl = ps.Jl;
+  const double* Q = ps.Q;
+  for (int j = 0; j < 3; ++j) {
+    grad_out[j] = (float)(Jl[j] * gr[0] + Jl[3 + j] * gr[1] + Jl[6 + j] * gr[2]);
+    grad_out[3 + j] = (float)(Q[j] * gr[0] + Q[3 + j] * gr[1] + Q[6 + j] * gr[2] + Jl[j] * gp[0] +
+                              Jl[3 + j] * gp[1] + Jl[6 + j] * gp[2]);
+  }
+}
+
+// One block per solve: the state of xi (exp, Q, the next step's bias corrections) by
+// four threads at once.
+__global__ void k_batch_pose_init(const float* xi, const float* adam_state, PoseState* states, double b1,
+                                  double b2) {
+  const int s = blockIdx.x;
+  const float* x = xi + 6 * (size_t)s;
+  const float* st = adam_state + 16 * (size_t)s;
+  switch (threadIdx.x) {
+    case 0: pose_state_exp(x, states + s); break;
+    case 32: pose_state_Q(x, states + s); break;
+    case 64: states[s].bc1 = bias_correction(b1, st); break;
+    case 96: states[s].bc2 = bias_correction(b2, st); break;
+    default: break;
+  }
 }
 
 // One block per solve: the solve's per-block pose partials summed in a fixed pattern
 // (thread i takes blocks i, i+256, ...; then a fixed tree), the SE(3) Jacobian
-// transpose, the Adam step and the next pose state. A solve's result depends only on
-// its own blocks, so it is the same whatever else is in the batch.
+// transpose and the Adam step with the state's cached Jacobian blocks and bias
+// corrections, then the state of the new xi by four threads at once. A solve's result
+// depends only on its own blocks, so it is the same whatever else is in the batch.
 __global__ void __launch_bounds__(256) k_batch_pose_update(const SceneDesc* descs, const double* partials,
                                                            float* xi, float* adam_state, PoseState* states,
                                                            const CfgsCounts* counts, int64_t cap, double lr,
                                                            double b1, double b2, double eps) {
   __shared__ double s_red[8][6];
+  __shared__ float s_x[6];
   if ((int64_t)counts->num_rendered > cap) return;  // overflowed iteration: no update
   const int s = blockIdx.x;
   const SceneDesc& sd = descs[s];
@@ -341,21 +387,32 @@ __global__ void __launch_bounds__(256) k_batch_pose_update(const SceneDesc* desc
     if (lane == 0) s_red[warp][k] = v;
   }
   __syncthreads();
+  float* x = xi + 6 * (size_t)s;
+  float* st = adam_state + 16 * (size_t)s;
+  PoseState* ps = states + s;
   if (threadIdx.x == 0) {
     double tot[kPosePartials];
     for (int k = 0; k < kPosePartials; ++k) tot[k] = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
       for (int k = 0; k < 6; ++k) tot[k] += s_red[w][k];
-    float* x = xi + 6 * (size_t)s;
     float grad[6];
-    pose_grad_from_sums(x, tot, grad);
-    adam_step6(x, grad, adam_state + 16 * (size_t)s, lr, b1, b2, eps);
-    pose_state_from_xi(x, states + s);
+    pose_grad_from_state(*ps, tot, grad);
+    adam_step6_bc(x, grad, st, lr, b1, b2, eps, ps->bc1, ps->bc2);
+    for (int k = 0; k < 6; ++k) s_x[k] = x[k];
+  }
+  __syncthreads();
+  switch (threadIdx.x) {
+    case 0: pose_state_exp(s_x, ps); break;
+    case 32: pose_state_Q(s_x, ps); break;
+    case 64: ps->bc1 = bias_correction(b1, st); break;
+    case 96: ps->bc2 = bias_correction(b2, st); break;
+    default: break;
   }
 }
 
-void launch_batch_pose_init(int count, const float* xi, PoseState* states, cudaStream_t st) {
-  k_batch_pose_init<<<div_up(count, 128), 128, 0, st>>>(count, xi, states);
+void launch_batch_pose_init(int count, const float* xi, const float* adam_state, PoseState* states, double b1,
+                            double b2, cudaStream_t st) {
+  k_batch_pose_init<<<count, 128, 0, st>>>(xi, adam_state, states, b1, b2);
 }
 void launch_batch_pose_update(int count, const SceneDesc* descs, const double* partials, float* xi,
                               float* adam_state, PoseState* states, const CfgsCounts* counts, int64_t cap, double lr,
