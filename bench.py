@@ -178,7 +178,10 @@ def run_ours(a) -> None:
     target = s.target
     HW = cam.width * cam.height
 
+    from cfgs import autotune
     from cfgs.loss import l1_loss_and_grad
+    sched = autotune.tune_rasterizer(rs, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None,
+                                     tuner=autotune.Autotuner())
     loss_buf = torch.empty((), dtype=torch.float32, device=dev)
     grad_buf = torch.empty_like(target)
     loss_scratch = torch.empty(4096, dtype=torch.uint8, device=dev)
@@ -244,6 +247,8 @@ def run_ours(a) -> None:
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{sc.n} SH{sc.sh_degree} Gaussians, {a.width}x{a.height}, "
                                    f"fwd + L1 loss + bwd", "num_rendered": int(K),
+                       "render_schedule": {"fwd_batch": sched.fwd_batch, "fwd_warps": sched.fwd_warps,
+                                           "bwd_batch": sched.bwd_batch},
                        "l2": "inputs larger than L2 (Gaussian parameters "
                              f"{sc.n * (44 + 12 * D) / 1e6:.0f} MB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
             "roofline": roofline, "phases": phases, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
@@ -442,8 +447,11 @@ def run_pose(a) -> None:
         xi, _ = pose.solve(prob, mode=mode)
         res[mode] = {"solves_per_s": round(sps, 4), "latency_s": [round(x, 4) for x in lat], "xi": xi}
 
+    from cfgs import autotune
+    tuner = autotune.Autotuner()
+
     def engine_solve():
-        return batch.BatchSolver([prob]).solve(300).xi[0]
+        return batch.BatchSolver([prob], autotune=tuner).solve(300).xi[0]
 
     engine_solve()
     lat = []
@@ -460,7 +468,8 @@ def run_pose(a) -> None:
     line = {"metric": "pose solves/s (640x360, 300 iterations)", "value": res["engine"]["solves_per_s"],
             "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "CF-3DGS relative pose solve, 230400 SH0 Gaussians, 640x360, 300 Adam iters",
-                       "path": "solve engine (cfgs_batch_iteration, CUDA graphs), setup included"},
+                       "path": "solve engine (cfgs_batch_iteration, CUDA graphs), setup included",
+                       "render_schedule": str(autotune.get_schedule())},
             "latency_p50_s": round(float(np.percentile(lat, 50)), 4),
             "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
             "plain_solves_per_s": res["plain"]["solves_per_s"],
@@ -481,8 +490,8 @@ def run_batch(a) -> None:
     from cfgs import batch, pose
     dev = torch.device("cuda", 0)
     specs, probs, _ = _pose_setup(dev, 64)
-    bs = batch.BatchSolver(probs)
-    bs.solve(300)
+    bs = batch.BatchSolver(probs, autotune=True)
+    bs.solve(300)  # tunes the render schedule for this batch shape (cached), untimed
     r = bs.solve(300)
     sample = max(2, min(8, a.steps))
     batch.solve_sequential(probs[:1], 300, "plain")
@@ -494,7 +503,7 @@ def run_batch(a) -> None:
             "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "64 CF-3DGS pose solves, N log-uniform [5e4,5e5], 3 resolutions, 300 iters",
                        "total_gaussians": int(sum(p.xyz.shape[0] for p in probs)), "num_rendered": r.num_rendered0,
-                       "graph_chunk": bs.graph_chunk},
+                       "graph_chunk": bs.graph_chunk, "render_schedule": str(bs.schedule)},
             "batch_seconds": round(r.seconds, 3), "ms_per_iteration": round(1000 * r.seconds / 300, 3),
             "plain_sequential_solves_per_s": round(plain_sps, 4), "plain_sample": sample,
             "fused_sequential_solves_per_s": round(sample / sum(latf), 4),

@@ -6,6 +6,8 @@ cfgs_batch_iteration call runs one iteration of every solve with one kernel laun
 stage, and a run of iterations is captured once in a CUDA graph and replayed. Per
 solve the arithmetic is that of the single fused solve (cfgs.pose.solve(mode="fused")),
 so a solve's result is the same alone, in any batch, and in the single-solve path.
+The render schedule (cfgs.autotune) can be tuned per batch shape; every schedule gives
+the same bits.
 """
 from __future__ import annotations
 
@@ -16,6 +18,7 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
+from . import autotune as autotune_mod
 from . import native
 from .pose import PoseProblem
 
@@ -38,10 +41,15 @@ class BatchSolver:
     one batch. Call solve(iters) to run them."""
 
     def __init__(self, problems: list[PoseProblem], lr: float = 1e-3, betas=(0.9, 0.999), eps: float = 1e-15,
-                 capacity_factor: float = 1.25, graph_chunk: int = 25, use_graph: bool = True):
+                 capacity_factor: float = 1.25, graph_chunk: int = 25, use_graph: bool = True, autotune=None):
+        """autotune: None (keep the process-wide render schedule), True (tune with the
+        default cache) or an autotune.Autotuner; when set, the render schedule of this
+        batch's shape is looked up or tuned on the batch itself before its iterations."""
         if not problems:
             raise ValueError("empty batch")
         self.problems = problems
+        self.tuner = (autotune_mod.Autotuner() if autotune is True else autotune) or None
+        self.schedule = None
         self.dev = problems[0].xyz.device
         self.lr, self.betas, self.eps = float(lr), betas, float(eps)
         self.capacity_factor = capacity_factor
@@ -163,6 +171,29 @@ class BatchSolver:
         self.xi.copy_(xi)
         self.adam.copy_(adam)
 
+    def _apply_schedule(self, args) -> None:
+        """Sets the render schedule for this batch's shape (tuning it on the batch when
+        the cache has none); the solves' state is left as it was."""
+        if self.tuner is None:
+            return
+        key = autotune_mod.batch_key(int(sum(int(p.xyz.shape[0]) for p in self.problems)), int(self.plan.num_tiles),
+                                     self.M)
+        sched = self.tuner.lookup(key)
+        if sched is None:
+            saved = (self.xi.clone(), self.adam.clone())
+            dev = self.dev
+
+            def run():
+                native.check(self.lib.cfgs_batch_iteration(C.byref(args), torch.cuda.current_stream(dev).cuda_stream),
+                             "cfgs_batch_iteration")
+
+            native.check(self.lib.cfgs_batch_init(C.byref(args), torch.cuda.current_stream(dev).cuda_stream),
+                         "cfgs_batch_init")
+            sched = self.tuner.tune(key, run)
+            self.load_state(*saved)
+        autotune_mod.set_schedule(sched)
+        self.schedule = sched
+
     def launch(self, iters: int) -> torch.cuda.Event:
         """Enqueues `iters` iterations of every solve from the current state (no reset)
         and returns an event that completes with them. The first call sizes the
@@ -175,6 +206,7 @@ class BatchSolver:
             self._cap_ready = True
         args = self._args()
         st = torch.cuda.current_stream(self.dev).cuda_stream
+        self._apply_schedule(args)
         native.check(self.lib.cfgs_batch_init(C.byref(args), st), "cfgs_batch_init")
         done = self._run_graph(args, iters) if (self.use_graph and iters >= self.graph_chunk) else 0
         for _ in range(iters - done):
@@ -222,6 +254,7 @@ class BatchSolver:
             self._alloc_instances(cap)
             args = self._args()
             st = torch.cuda.current_stream(self.dev).cuda_stream
+            self._apply_schedule(args)
             native.check(self.lib.cfgs_batch_init(C.byref(args), st), "cfgs_batch_init")
             t0 = time.perf_counter()
             if self.use_graph and iters >= self.graph_chunk:

@@ -74,6 +74,10 @@ class Counts(C.Structure):
     _fields_ = [("num_rendered", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class RenderSchedule(C.Structure):
+    _fields_ = [("fwd_batch", C.c_int32), ("fwd_warps", C.c_int32), ("bwd_batch", C.c_int32), ("reserved", C.c_int32)]
+
+
 class BatchScene(C.Structure):
     _fields_ = [("image_width", C.c_int32), ("image_height", C.c_int32), ("tanfovx", C.c_float),
                 ("tanfovy", C.c_float), ("viewmatrix", _fp), ("projmatrix", _fp), ("campos", _fp), ("bg", _fp),
@@ -141,6 +145,8 @@ EXPORTS = {
     "cfgs_ssim_scratch_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     "cfgs_ssim_forward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_ssim_backward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "cfgs_set_render_schedule": (C.c_int, [C.POINTER(RenderSchedule)]),
+    "cfgs_get_render_schedule": (None, [C.POINTER(RenderSchedule)]),
     "cfgs_l1_loss_scratch_bytes": (C.c_size_t, [C.c_int64]),
     "cfgs_l1_loss_forward": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, _vp, _vp]),
     "cfgs_l1_loss_backward": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, _vp]),

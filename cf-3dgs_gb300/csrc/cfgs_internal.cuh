@@ -216,6 +216,7 @@ struct SceneDesc {
 };
 
 struct SingleScene {
+  static constexpr bool kBatched = false;
   SceneDesc d;
   __device__ __forceinline__ const SceneDesc& for_block(int) const { return d; }
   __device__ __forceinline__ const SceneDesc& for_tile(int) const { return d; }
@@ -223,6 +224,7 @@ struct SingleScene {
 };
 
 struct SceneTable {
+  static constexpr bool kBatched = true;
   const SceneDesc* d;
   const int32_t* block_scene;  // preprocess block -> scene
   const int32_t* tile_scene;   // global tile -> scene

@@ -114,6 +114,9 @@ template <class Scenes>
 void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st);
 template <class Scenes>
 void launch_preprocess_bwd(const PreBwdArgs<Scenes>& a, int blocks, cudaStream_t st);
+// The process-wide render schedule (cfgs_set_render_schedule), read at launch time.
+CfgsRenderSchedule render_schedule();
+
 void launch_batch_pose_init(int count, const float* xi, const float* adam_state, PoseState* states, double b1,
                             double b2, cudaStream_t st);
 void launch_batch_pose_update(int count, const SceneDesc* descs, const double* partials, float* xi,

@@ -15,8 +15,6 @@
 
 namespace cfgs {
 
-constexpr int kBwdBatch = 64;
-static_assert(kBwdBatch % 32 == 0, "batches are whole ballot words");
 constexpr int kBwdThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
 constexpr int kWarps = kBwdThreads / 32;
 
@@ -206,9 +204,13 @@ __device__ __forceinline__ void finish_record(float4* rec, const float (&s)[10],
 // lane: rows r and r + 4) and exact shortcuts (box_may_contribute per warp and
 // instance, alpha_threshold per pixel). A lane adds its two pixels' terms before the
 // warp reduction; the cross-warp sum of an instance adds only the warps that kept it
-// (the others' terms are exact zeros).
-template <class Scenes, bool DEPTH>
+// (the others' terms are exact zeros). BATCH instances are staged per round; the
+// records do not depend on it (each instance's sums are formed the same way whatever
+// batch it is staged in), so the batch is a schedule choice.
+template <class Scenes, bool DEPTH, int BATCH>
 __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Scenes> a) {
+  static_assert(BATCH % 32 == 0 && BATCH <= kBwdThreads, "whole ballot words, one staged instance per thread");
+  constexpr int kBwdBatch = BATCH;
   __shared__ float4 s_xyt[kBwdBatch];
   __shared__ float4 s_co[kBwdBatch];
   __shared__ float4 s_rgbd[kBwdBatch];
@@ -321,10 +323,22 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
   }
 }
 
+template <class Scenes, bool DEPTH>
+void launch_render_bwd_depth(const RenderBwdArgs<Scenes>& a, int tiles, int batch, cudaStream_t st) {
+  if (batch == 32) k_render_bwd<Scenes, DEPTH, 32><<<tiles, kBwdThreads, 0, st>>>(a);
+  else if (batch == 128) k_render_bwd<Scenes, DEPTH, 128><<<tiles, kBwdThreads, 0, st>>>(a);
+  else k_render_bwd<Scenes, DEPTH, 64><<<tiles, kBwdThreads, 0, st>>>(a);
+}
+
 template <class Scenes>
 void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st) {
-  if (a.dL_ddepth) k_render_bwd<Scenes, true><<<tiles, kBwdThreads, 0, st>>>(a);
-  else k_render_bwd<Scenes, false><<<tiles, kBwdThreads, 0, st>>>(a);
+  const int batch = render_schedule().bwd_batch;
+  if constexpr (Scenes::kBatched) {  // batched solves never ask for depth gradients
+    launch_render_bwd_depth<Scenes, false>(a, tiles, batch, st);
+  } else {
+    if (a.dL_ddepth) launch_render_bwd_depth<Scenes, true>(a, tiles, batch, st);
+    else launch_render_bwd_depth<Scenes, false>(a, tiles, batch, st);
+  }
 }
 template void launch_render_bwd<SingleScene>(const RenderBwdArgs<SingleScene>&, int, cudaStream_t);
 template void launch_render_bwd<SceneTable>(const RenderBwdArgs<SceneTable>&, int, cudaStream_t);

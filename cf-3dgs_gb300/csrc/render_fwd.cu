@@ -5,14 +5,17 @@
 // descriptor table for batched solves); the arithmetic is the same for both.
 // Compiled with -fmad=false; the fmaf() calls are the only fused operations, and the
 // CPU oracle performs the same sequence.
+#include <mutex>
+
 #include "cfgs_internal.cuh"
 #include "kernels.cuh"
 
 namespace cfgs {
 
-constexpr int kRenderThreads = 128;  // 2 pixels per thread, 4 warps per 16x16 tile
+// Launch schedules (cfgs_set_render_schedule): kRenderBatch instances staged per round
+// and 4 or 8 warps per tile. Every schedule gives bit-identical outputs: each pixel sees
+// the same instances in the same order with the same arithmetic.
 constexpr int kRenderBatch = 128;
-static_assert(kRenderBatch % kRenderThreads == 0 && kRenderBatch % 32 == 0, "whole staging rounds");
 
 // Front-to-back state of a lane's two pixels (.x: row r, .y: row r + 4) and one
 // compositing step of both: the published loop body per pixel, with the exponential
@@ -67,10 +70,11 @@ __device__ __forceinline__ void composite_pair(PairFwd& p, float pxf, float2 pyf
   }
 }
 
-// One block of 128 threads per 16x16 tile; warp w covers the 8x8 pixel box
-// (8 (w & 1), 8 (w >> 1)) and each lane two pixels of it, rows r and r + 4. Batches of
-// kRenderBatch instances are gathered into shared memory, kRenderBatch / kRenderThreads
-// per thread (per-Gaussian data stays L2-resident).
+// One block of 32 WARPS threads per 16x16 tile. With 4 warps, warp w covers the 8x8
+// pixel box (8 (w & 1), 8 (w >> 1)) and each lane two pixels of it, rows r and r + 4;
+// with 8 warps, warp w covers the 8x4 box (8 (w & 1), 4 (w >> 1)) and each lane one
+// pixel (the pair's second pixel is never inside). Batches of BATCH instances are
+// gathered into shared memory (per-Gaussian data stays L2-resident).
 // Two exact shortcuts skip work whose outcome is known: each warp keeps only the
 // instances whose alpha >= 1/255 ellipse can reach its box (box_may_contribute, one test
 // per instance and warp), and a pixel skips the exponential when the exponent lies
@@ -78,31 +82,33 @@ __device__ __forceinline__ void composite_pair(PairFwd& p, float pxf, float2 pyf
 // algorithm, so every output — contributor counts included, which count positions in
 // the tile's list — is what the plain per-pixel loop gives. Compositing runs front to
 // back; a warp stops when its pixels are saturated and the block when all are.
-template <class Scenes>
-__global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes> a) {
-  __shared__ float4 s_xyt[kRenderBatch];   // (x, y, alpha threshold, -)
-  __shared__ float4 s_co[kRenderBatch];    // (ca, cb, cc, opacity)
-  __shared__ float4 s_rgbd[kRenderBatch];
+template <class Scenes, int BATCH, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_render_fwd(RenderArgs<Scenes> a) {
+  static_assert(BATCH % 32 == 0 && (WARPS == 4 || WARPS == 8), "whole ballot words; 8x8 or 8x4 warp boxes");
+  constexpr int kThreads = 32 * WARPS;
+  constexpr int kBoxRows = WARPS == 4 ? 8 : 4;
+  __shared__ float4 s_xyt[BATCH];   // (x, y, alpha threshold, -)
+  __shared__ float4 s_co[BATCH];    // (ca, cb, cc, opacity)
+  __shared__ float4 s_rgbd[BATCH];
   if ((int64_t)a.counts->num_rendered > a.cap) return;
   const int tile = blockIdx.x;
   const SceneDesc& sd = a.scenes.for_tile(tile);
   const int lt = tile - sd.tile_base;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int bx0 = (lt % sd.grid_x) * kTileX + (warp & 1) * 8;
-  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * 8;
+  const int by0 = (lt / sd.grid_x) * kTileY + (warp >> 1) * kBoxRows;
   const int px = bx0 + (lane & 7), py0 = by0 + (lane >> 3), py1 = py0 + 4;
-  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + 7);
-  const bool in0 = px < sd.W && py0 < sd.H, in1 = px < sd.W && py1 < sd.H;
+  const float bxf0 = (float)bx0, bxf1 = (float)(bx0 + 7), byf0 = (float)by0, byf1 = (float)(by0 + kBoxRows - 1);
+  const bool in0 = px < sd.W && py0 < sd.H, in1 = WARPS == 4 && px < sd.W && py1 < sd.H;
   const float pxf = (float)px, pyf0 = (float)py0, pyf1 = (float)py1;
   const uint32_t lo = a.tile_range[tile];
   const int n = (int)(a.tile_range[tile + 1] - lo);
   PairFwd pp{splat2(1.0f), splat2(0.0f), splat2(0.0f), splat2(0.0f), splat2(0.0f), 0u, 0u, !in0, !in1};
   const float2 pyf = make_float2(pyf0, pyf1);
-  for (int base = 0; base < n; base += kRenderBatch) {
-    if (__syncthreads_count(pp.done0 && pp.done1) == kRenderThreads) break;
+  for (int base = 0; base < n; base += BATCH) {
+    if (__syncthreads_count(pp.done0 && pp.done1) == kThreads) break;
 #pragma unroll
-    for (int k = 0; k < kRenderBatch / kRenderThreads; ++k) {
-      const int j = k * kRenderThreads + threadIdx.x;
+    for (int j = threadIdx.x; j < BATCH; j += kThreads) {
       const int i = base + j;
       if (i < n) {
         uint32_t g = a.sorted_gid[lo + i];
@@ -114,10 +120,10 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes
       }
     }
     __syncthreads();
-    const int cnt = min(kRenderBatch, n - base);
-    uint32_t keep[kRenderBatch / 32];
+    const int cnt = min(BATCH, n - base);
+    uint32_t keep[BATCH / 32];
 #pragma unroll
-    for (int r = 0; r < kRenderBatch / 32; ++r) {
+    for (int r = 0; r < BATCH / 32; ++r) {
       const int j = r * 32 + lane;
       bool k = false;
       if (j < cnt) {
@@ -128,7 +134,7 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes
       keep[r] = __ballot_sync(0xffffffffu, k);
     }
 #pragma unroll
-    for (int r = 0; r < kRenderBatch / 32; ++r) {
+    for (int r = 0; r < BATCH / 32; ++r) {
       if (__all_sync(0xffffffffu, pp.done0 && pp.done1)) break;
       uint32_t mk = keep[r];
       while (mk) {
@@ -162,14 +168,51 @@ __global__ void __launch_bounds__(kRenderThreads) k_render_fwd(RenderArgs<Scenes
 
 template <class Scenes>
 void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st) {
-  k_render_fwd<Scenes><<<tiles, kRenderThreads, 0, st>>>(a);
+  const CfgsRenderSchedule rs = render_schedule();
+  if (rs.fwd_warps == 8) {
+    if (rs.fwd_batch == 256) k_render_fwd<Scenes, 256, 8><<<tiles, 256, 0, st>>>(a);
+    else k_render_fwd<Scenes, 128, 8><<<tiles, 256, 0, st>>>(a);
+  } else {
+    if (rs.fwd_batch == 64) k_render_fwd<Scenes, 64, 4><<<tiles, 128, 0, st>>>(a);
+    else if (rs.fwd_batch == 256) k_render_fwd<Scenes, 256, 4><<<tiles, 128, 0, st>>>(a);
+    else k_render_fwd<Scenes, kRenderBatch, 4><<<tiles, 128, 0, st>>>(a);
+  }
 }
 template void launch_render_fwd<SingleScene>(const RenderArgs<SingleScene>&, int, cudaStream_t);
 template void launch_render_fwd<SceneTable>(const RenderArgs<SceneTable>&, int, cudaStream_t);
 
 }  // namespace cfgs
 
+namespace cfgs {
+
+namespace {
+std::mutex g_schedule_mu;
+CfgsRenderSchedule g_schedule{kRenderBatch, 4, 64, 0};
+}  // namespace
+
+CfgsRenderSchedule render_schedule() {
+  std::lock_guard<std::mutex> lk(g_schedule_mu);
+  return g_schedule;
+}
+
+}  // namespace cfgs
+
 using namespace cfgs;
+
+extern "C" int cfgs_set_render_schedule(const CfgsRenderSchedule* s) {
+  if (!s) return CFGS_ERR_INVALID_ARGUMENT;
+  const bool fwd_ok = s->fwd_warps == 4 ? (s->fwd_batch == 64 || s->fwd_batch == 128 || s->fwd_batch == 256)
+                                        : (s->fwd_warps == 8 && (s->fwd_batch == 128 || s->fwd_batch == 256));
+  const bool bwd_ok = s->bwd_batch == 32 || s->bwd_batch == 64 || s->bwd_batch == 128;
+  if (!fwd_ok || !bwd_ok) return CFGS_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(g_schedule_mu);
+  g_schedule = CfgsRenderSchedule{s->fwd_batch, s->fwd_warps, s->bwd_batch, 0};
+  return CFGS_OK;
+}
+
+extern "C" void cfgs_get_render_schedule(CfgsRenderSchedule* s) {
+  if (s) *s = render_schedule();
+}
 
 extern "C" int cfgs_composite_forward(const CfgsSettings* s, int32_t num_gaussians, const void* geom, const void* image,
                                       const void* binning, int64_t capacity, float* out_color, float* out_depth,

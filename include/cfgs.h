@@ -263,6 +263,23 @@ int cfgs_ssim_forward(int32_t channels, int32_t height, int32_t width, const flo
 int cfgs_ssim_backward(int32_t channels, int32_t height, int32_t width, const float* img1, const float* img2,
                        const void* scratch, const float* dL_dmean, float* dL_dimg1, void* stream);
 
+/* ---- render schedule -----------------------------------------------------------------
+ * Launch shape of the two per-tile render kernels. Every schedule gives bit-identical
+ * results (each pixel sees the same instances in the same order with the same
+ * arithmetic, and each instance's gradient record is summed the same way), so the
+ * choice is a pure performance one; cfgs/autotune.py picks it by timing.
+ *   fwd_batch: instances staged per round in the forward: 64, 128 or 256
+ *   fwd_warps: warps per tile in the forward: 4 (8x8 pixel boxes, two pixels per
+ *              lane) or 8 (8x4 boxes, one pixel per lane; fwd_batch 128 or 256)
+ *   bwd_batch: instances staged per round in the backward: 32, 64 or 128
+ * Process-wide; each launch reads it when it is issued (a captured CUDA graph keeps the
+ * schedule of its capture). Default {128, 4, 64}. */
+typedef struct CfgsRenderSchedule {
+  int32_t fwd_batch, fwd_warps, bwd_batch, reserved;
+} CfgsRenderSchedule;
+int cfgs_set_render_schedule(const CfgsRenderSchedule* schedule); /* INVALID_ARGUMENT if unsupported */
+void cfgs_get_render_schedule(CfgsRenderSchedule* schedule);
+
 /* ---- L1 photometric loss ------------------------------------------------------------
  * mean |x - target| over n floats (utils/loss_utils.py:15-16, trainer/losses.py:139-140),
  * of clamp(x, 0, 1) when clamp != 0 (the pose solve clamps the render before its loss:
