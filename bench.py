@@ -124,13 +124,42 @@ def phase_bytes(N: int, K: int, HW: int, D: int) -> dict:
     }
 
 
+# FP32 operations per (pixel, Gaussian) evaluation of the plain algorithm (an
+# exponential counted as one): forward ~11 + exp, backward ~40 + exp.
+ALU_OPS_PER_EVAL = {"composite": 12, "render_bwd": 41}
+
+
+def alu_roofline(E: int, phase_ms: dict, pb: dict, peaks: dict) -> dict:
+    """ALU roofline of the two render kernels: E = sum of the per-pixel contributor
+    counts (the evaluations of the plain per-pixel loop), E x ops per evaluation over the
+    kernel time against the nominal FP32 peak (SMs x 128 lanes x 2 flops x max clock;
+    no measured FP32 peak is available). Also the iteration's lower bound with each
+    phase at its tighter bound (bytes / HBM or ops / FP32) against the measured phases."""
+    import torch
+    props = torch.cuda.get_device_properties(0)
+    mhz = peaks.get("sm_max_mhz") or 2070.0
+    peak = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+    out = {"E": E, "fp32_peak_tflops": round(peak, 2), "peak_source": "nominal (SMs x 128 x 2 x max clock)"}
+    t_min = 0.0
+    for k, ms in phase_ms.items():
+        t_hbm = pb[k] / (peaks["hbm_gbs"] * 1e9)
+        t_alu = E * ALU_OPS_PER_EVAL[k] / (peak * 1e12) if k in ALU_OPS_PER_EVAL else 0.0
+        t_min += max(t_hbm, t_alu)
+        if k in ALU_OPS_PER_EVAL:
+            tf = E * ALU_OPS_PER_EVAL[k] / (ms / 1000.0) / 1e12
+            out[k] = {"achieved_tflops": round(tf, 3), "frac": round(tf / peak, 4)}
+    out["iteration_bound_ms"] = round(t_min * 1000.0, 4)
+    out["iteration_frac"] = round(t_min * 1000.0 / sum(phase_ms.values()), 4)
+    return out
+
+
 def _peaks() -> dict:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured", "sm_max_mhz": float(d.get("sm_max_mhz", 2070.0))}
     except Exception:
-        return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": 6800.0, "source": "fallback", "sm_max_mhz": 2070.0}
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
@@ -186,6 +215,8 @@ def run_ours(a) -> None:
     grad_buf = torch.empty_like(target)
     loss_scratch = torch.empty(4096, dtype=torch.uint8, device=dev)
 
+    last_state = [None]
+
     def step(timers=None):
         color, radii, depth, alpha, st = raster.forward(rs, s.means3D, s.opacities, s.shs, None, s.scales,
                                                         s.rotations, None, timers=timers)
@@ -193,6 +224,7 @@ def run_ours(a) -> None:
         loss, g = l1_loss_and_grad(color, target, clamp=True, out=loss_buf, grad_out=grad_buf, scratch=loss_scratch)
         raster.backward(rs, st, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None, g, None, None,
                         timers=timers)
+        last_state[0] = st
         return loss, st.num_rendered
 
     for _ in range(max(a.warmup, 0)):
@@ -231,6 +263,8 @@ def run_ours(a) -> None:
                 "algorithmic_bytes_per_launch": pb[dom]}
     phases = {k: {"ms": round(v, 4), "share": round(v / sum(phase_ms.values()), 4),
                   "hbm_frac": round(pb[k] / (v / 1000.0) / 1e9 / peaks["hbm_gbs"], 5)} for k, v in phase_ms.items()}
+    E = int(raster.inspect_state(last_state[0], cam.width, cam.height)["n_contrib"].to(torch.int64).sum())
+    render_alu = alu_roofline(E, phase_ms, pb, peaks)
 
     e2e = None
     if not a.no_e2e:
@@ -251,7 +285,8 @@ def run_ours(a) -> None:
                                            "bwd_batch": sched.bwd_batch},
                        "l2": "inputs larger than L2 (Gaussian parameters "
                              f"{sc.n * (44 + 12 * D) / 1e6:.0f} MB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
-            "roofline": roofline, "phases": phases, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "roofline": roofline, "phases": phases, "render_alu": render_alu, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clk,
             "gpu_launches": (raster.kernel_launches(sc.camera.width, sc.camera.height)["total"] + 2) * a.steps,
         }
         print(json.dumps(line), flush=True)
