@@ -431,13 +431,9 @@ namespace {
 
 template <int CHUNK, bool DEPTH>
 int launch_pass(const SortPass& p, cudaStream_t st) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(k_sort_scatter<CHUNK, DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)ScatterSmem<CHUNK>::bytes(true)) != cudaSuccess)
-      return CFGS_ERR_LAUNCH;
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> smem_set{0};
+  if (!ensure_dynamic_smem(k_sort_scatter<CHUNK, DEPTH>, (int)ScatterSmem<CHUNK>::bytes(true), smem_set))
+    return CFGS_ERR_LAUNCH;
   const int grid = (int)p.num_chunks;
   k_sort_count<CHUNK, DEPTH><<<grid, kSortThreads, 0, st>>>(p);
   k_sort_scan<CHUNK><<<1 << p.bits, 1024, 0, st>>>(p);

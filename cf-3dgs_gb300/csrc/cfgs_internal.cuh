@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../../include/cfgs.h"
 
 namespace cfgs {
@@ -20,6 +22,21 @@ constexpr int kMaxShCoeffs = 16;  // SH degree 3
 // Workspace layouts. Every array starts on a 256-byte boundary.
 // ---------------------------------------------------------------------------
 __host__ __device__ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Raises a kernel's dynamic shared-memory limit to `bytes` on the current device, once
+// per device (a function attribute belongs to the device's context, so one flag per
+// process would leave a second GPU of the process without it). `done` is the kernel's
+// own set of device bits; devices past 63 set the attribute on every call.
+template <class Kernel>
+inline bool ensure_dynamic_smem(Kernel* kernel, int bytes, std::atomic<uint64_t>& done) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  const uint64_t bit = dev < 64 ? (uint64_t)1 << dev : 0;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return true;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return false;
+  done.fetch_or(bit, std::memory_order_acq_rel);
+  return true;
+}
 
 // Binning sorts (stable LSD radix, at most 8 bits per pass) work on chunks of
 // elements: kDepthChunk for the depth sort of the Gaussians (4 passes), kTileChunk for

@@ -507,11 +507,8 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
 template <class Scenes>
 void launch_preprocess_bwd(const PreBwdArgs<Scenes>& a, int blocks, cudaStream_t st) {
   constexpr int kShBulkBytes = 256 * 3 * kMaxShCoeffs * (int)sizeof(float);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_preprocess_bwd<Scenes>, cudaFuncAttributeMaxDynamicSharedMemorySize, kShBulkBytes);
-    attr_set = true;
-  }
+  static std::atomic<uint64_t> smem_set{0};
+  ensure_dynamic_smem(k_preprocess_bwd<Scenes>, kShBulkBytes, smem_set);  // a failure surfaces as a launch error
   k_preprocess_bwd<Scenes><<<blocks, 256, a.sh_bulk ? kShBulkBytes : 0, st>>>(a);
 }
 template void launch_preprocess_bwd<SingleScene>(const PreBwdArgs<SingleScene>&, int, cudaStream_t);
