@@ -117,6 +117,7 @@ def phase_bytes(N: int, K: int, HW: int, D: int) -> dict:
     params = N * (12 + 4 + 12 * D + 12 + 16)
     return {
         "preprocess": params + N * (8 + 16 + 16 + 8 + 4 + 1 + 4),
+        "depth_sort": N * (4 * 16 + 8),
         "bin": N * (4 + 8 + 4 + 4) + K * (8 + 4) + K * (8 + 4 + 8),
         "composite": K * (4 + 8 + 16 + 16) + HW * (12 + 4 + 4 + 4 + 4),
         "render_bwd": K * (4 + 4 + 8 + 16 + 16 + 48) + HW * (4 + 4 + 12 + 4 + 4),

@@ -117,6 +117,8 @@ EXPORTS = {
     "cfgs_backward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, _vp, C.c_int64, _vp,
                                 _vp, _vp, _vp, C.POINTER(Gradients), _vp]),
     "cfgs_bin_forward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, C.c_int64, _vp]),
+    "cfgs_depth_order": (C.c_int, [C.c_int32, _vp, _vp]),
+    "cfgs_bin_instances": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, C.c_int64, _vp]),
     "cfgs_composite_forward": (C.c_int, [C.POINTER(Settings), C.c_int32, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp,
                                          _vp]),
     "cfgs_render_backward": (C.c_int, [C.POINTER(Settings), C.c_int32, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp, _vp,

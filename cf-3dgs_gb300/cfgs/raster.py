@@ -105,6 +105,27 @@ class _Timed:
             self.timers.setdefault(self.name, []).append(self.ev)
 
 
+_SIDE_STREAMS: dict = {}
+
+
+def _read_counts_after(image: torch.Tensor, ready: torch.cuda.Event, dev) -> native.Counts:
+    """The CfgsCounts at the head of an image workspace, copied to pinned host memory
+    on a side stream once `ready` has completed (work enqueued after it on the current
+    stream keeps running). Waits for that copy only."""
+    side = _SIDE_STREAMS.get(dev)
+    if side is None:
+        side = _SIDE_STREAMS[dev] = torch.cuda.Stream(dev)
+    host = torch.empty(C.sizeof(native.Counts), dtype=torch.uint8, pin_memory=True)
+    with torch.cuda.stream(side):
+        side.wait_event(ready)
+        host.copy_(image[: host.numel()], non_blocking=True)
+        done = torch.cuda.Event()
+        done.record(side)
+    image.record_stream(side)
+    done.synchronize()
+    return native.Counts.from_buffer_copy(host.numpy().tobytes())
+
+
 def forward(rs, means3D, opacities, shs, colors_precomp, scales, rotations, cov3D_precomp, timers=None):
     """Runs both forward phases. Returns (color, radii, depth, alpha, ForwardState)."""
     lib = native.load()
@@ -123,8 +144,13 @@ def forward(rs, means3D, opacities, shs, colors_precomp, scales, rotations, cov3
     with _Timed(timers, "preprocess"):
         native.check(lib.cfgs_preprocess_forward(C.byref(s), C.byref(g), geom.data_ptr(), image.data_ptr(),
                                                  radii.data_ptr() if N else None, st), "cfgs_preprocess_forward")
-    counts = native.Counts()
-    native.check(lib.cfgs_read_counts(image.data_ptr(), C.byref(counts), st), "cfgs_read_counts")
+    # K is final here; the depth sort does not need it, so it is enqueued before the host
+    # waits for K (read on a side stream), and keeps the GPU busy meanwhile.
+    k_ready = torch.cuda.Event()
+    k_ready.record(torch.cuda.current_stream(dev))
+    with _Timed(timers, "depth_sort"):
+        native.check(lib.cfgs_depth_order(N, geom.data_ptr(), st), "cfgs_depth_order")
+    counts = _read_counts_after(image, k_ready, dev)
     if counts.flags & native.FLAG_FRUSTUM_VIOLATION:
         raise RuntimeError("prefiltered=True but a Gaussian lies at view z <= 0.2 (outside the frustum)")
     if counts.flags & native.FLAG_CAPACITY_OVERFLOW:
@@ -135,8 +161,8 @@ def forward(rs, means3D, opacities, shs, colors_precomp, scales, rotations, cov3
     depth = torch.empty((1, H, W), dtype=torch.float32, device=dev)
     alpha = torch.empty((1, H, W), dtype=torch.float32, device=dev)
     with _Timed(timers, "bin"):
-        native.check(lib.cfgs_bin_forward(C.byref(s), C.byref(g), geom.data_ptr(), image.data_ptr(),
-                                          binning.data_ptr(), K, st), "cfgs_bin_forward")
+        native.check(lib.cfgs_bin_instances(C.byref(s), C.byref(g), geom.data_ptr(), image.data_ptr(),
+                                            binning.data_ptr(), K, st), "cfgs_bin_instances")
     with _Timed(timers, "composite"):
         native.check(lib.cfgs_composite_forward(C.byref(s), N, geom.data_ptr(), image.data_ptr(), binning.data_ptr(),
                                                 K, color.data_ptr(), depth.data_ptr(), alpha.data_ptr(), st),

@@ -453,11 +453,9 @@ void tile_sort_plan(int64_t num_tiles, int* passes, int* width) {
   *width = (bits + *passes - 1) / *passes;
 }
 
-template <class Scenes>
-int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {
-  const GeomView& gv = a.geom;
-  const BinningView& bv = a.bin;
-  const int64_t slots = a.total_slots;
+// Step 1 of the binning, which needs no instance capacity: the depth order of the
+// Gaussians and their instance counts per 256 in that order.
+int launch_depth_order(const GeomView& gv, int64_t slots, cudaStream_t st) {
   if (slots > 0) {
     // 1. depth sort of the Gaussians: geometry -> 0 -> 1 -> 0 -> depth_val[1]
     int src = -1;
@@ -482,9 +480,21 @@ int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {
       if (s != CFGS_OK) return s;
       src = dst;
     }
-    // 2. emission in depth order
     const int rank_blocks = (int)((slots + kPreprocessBlock - 1) / kPreprocessBlock);
     k_rank_sums<<<rank_blocks, kPreprocessBlock, 0, st>>>(gv.depth_val[1], gv.touched, slots, gv.rank_sums);
+  }
+  return CFGS_OK;
+}
+
+// Steps 2-3, after launch_depth_order: emission in depth order, tile sort, tile ranges.
+template <class Scenes>
+int launch_instances(const BinArgs<Scenes>& a, cudaStream_t st) {
+  const GeomView& gv = a.geom;
+  const BinningView& bv = a.bin;
+  const int64_t slots = a.total_slots;
+  if (slots > 0) {
+    // 2. emission in depth order
+    const int rank_blocks = (int)((slots + kPreprocessBlock - 1) / kPreprocessBlock);
     EmitArgs<Scenes> e;
     e.scenes = a.scenes;
     e.total_slots = slots;
@@ -527,6 +537,12 @@ int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {
   k_tile_ranges<<<1, 1024, 0, st>>>(a.tile_count, a.tile_range, a.num_tiles);
   return CFGS_OK;
 }
+
+template <class Scenes>
+int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {
+  const int s = launch_depth_order(a.geom, a.total_slots, st);
+  return s != CFGS_OK ? s : launch_instances(a, st);
+}
 template int launch_binning<SingleScene>(const BinArgs<SingleScene>&, cudaStream_t);
 
 // Stable LSD radix sort of n (key, value) pairs by the low `bits` key bits, passes of at
@@ -567,25 +583,58 @@ template int launch_binning<SceneTable>(const BinArgs<SceneTable>&, cudaStream_t
 
 using namespace cfgs;
 
-extern "C" int cfgs_bin_forward(const CfgsSettings* s, const CfgsGaussians* g, void* geom, void* image, void* binning,
-                                int64_t capacity, void* stream) {
+namespace {
+
+// The single-scene binning arguments of the drop-in path.
+int single_bin_args(const CfgsSettings* s, const CfgsGaussians* g, void* geom, void* image, void* binning,
+                    int64_t capacity, BinArgs<SingleScene>* a) {
   if (!s || !g || !geom || !image || !binning || capacity < 0) return CFGS_ERR_INVALID_ARGUMENT;
   if (s->image_width <= 0 || s->image_height <= 0 || g->num_gaussians < 0) return CFGS_ERR_INVALID_ARGUMENT;
   if (capacity > 0x7fffffffll) return CFGS_ERR_TOO_LARGE;
-  cudaStream_t st = (cudaStream_t)stream;
   ImageLayout IL(s->image_width, s->image_height);
   ImageView iv(image, s->image_width, s->image_height);
+  a->scenes.d = single_scene_desc(s, g->num_gaussians, g->sh_coeffs);
+  a->total_slots = g->num_gaussians;
+  a->geom = GeomView(geom, g->num_gaussians);
+  a->bin = BinningView(binning, capacity);
+  a->cap = capacity;
+  a->counts = iv.counts;
+  a->num_tiles = IL.num_tiles;
+  a->tile_count = iv.tile_count;
+  a->tile_range = iv.tile_range;
+  return CFGS_OK;
+}
+
+}  // namespace
+
+extern "C" int cfgs_bin_forward(const CfgsSettings* s, const CfgsGaussians* g, void* geom, void* image, void* binning,
+                                int64_t capacity, void* stream) {
   BinArgs<SingleScene> a;
-  a.scenes.d = single_scene_desc(s, g->num_gaussians, g->sh_coeffs);
-  a.total_slots = g->num_gaussians;
-  a.geom = GeomView(geom, g->num_gaussians);
-  a.bin = BinningView(binning, capacity);
-  a.cap = capacity;
-  a.counts = iv.counts;
-  a.num_tiles = IL.num_tiles;
-  a.tile_count = iv.tile_count;
-  a.tile_range = iv.tile_range;
-  int status = launch_binning(a, st);
+  int status = single_bin_args(s, g, geom, image, binning, capacity, &a);
+  if (status != CFGS_OK) return status;
+  cudaStream_t st = (cudaStream_t)stream;
+  status = launch_binning(a, st);
+  if (status != CFGS_OK) return status;
+  CFGS_CHECK_LAUNCH(s->debug, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_depth_order(int32_t num_gaussians, void* geom, void* stream) {
+  if (num_gaussians < 0 || (num_gaussians > 0 && !geom)) return CFGS_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int status = launch_depth_order(GeomView(geom, num_gaussians), num_gaussians, st);
+  if (status != CFGS_OK) return status;
+  CFGS_CHECK_LAUNCH(0, st);
+  return CFGS_OK;
+}
+
+extern "C" int cfgs_bin_instances(const CfgsSettings* s, const CfgsGaussians* g, void* geom, void* image,
+                                  void* binning, int64_t capacity, void* stream) {
+  BinArgs<SingleScene> a;
+  int status = single_bin_args(s, g, geom, image, binning, capacity, &a);
+  if (status != CFGS_OK) return status;
+  cudaStream_t st = (cudaStream_t)stream;
+  status = launch_instances(a, st);
   if (status != CFGS_OK) return status;
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;

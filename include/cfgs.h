@@ -166,6 +166,15 @@ int cfgs_composite_forward(const CfgsSettings* settings, int32_t num_gaussians, 
                            const void* image, const void* binning, int64_t capacity, float* out_color,
                            float* out_depth, float* out_alpha, void* stream);
 
+/* cfgs_bin_forward in two steps, so that the part that does not depend on K can run
+ * while the host reads K: cfgs_depth_order (after cfgs_preprocess_forward: the depth
+ * sort of the Gaussians, in the geom workspace) and cfgs_bin_instances (after it, with
+ * the binning workspace sized for K: instance emission, tile sort, tile ranges).
+ * cfgs_depth_order + cfgs_bin_instances = cfgs_bin_forward. */
+int cfgs_depth_order(int32_t num_gaussians, void* geom, void* stream);
+int cfgs_bin_instances(const CfgsSettings* settings, const CfgsGaussians* gaussians, void* geom, void* image,
+                       void* binning, int64_t capacity, void* stream);
+
 /* ---- rasteriser backward ------------------------------------------------------
  * Replaces upstream rasterize_gaussians_backward (render backward, computeCov2D
  * backward, preprocess backward). dL_dcolor [3,H,W]; dL_ddepth and dL_dalpha

@@ -36,6 +36,7 @@ def test_workspace_sizes_and_layouts():
     vals = [g[k] for k in native.GEOM_FIELDS]
     assert vals == sorted(vals) and all(v % 256 == 0 for v in vals)
     im = native.image_layout(1920, 1080)
+    assert im["counts"] == 0  # raster.forward reads the counts from the workspace's first bytes
     assert im["total"] == lib.cfgs_image_bytes(1920, 1080)
     assert im["n_contrib"] - im["final_T"] >= 1920 * 1080 * 4
     b = native.binning_layout(12345)
