@@ -249,6 +249,9 @@ class RasterizeGaussiansFn(torch.autograd.Function):
         ctx.has = (sh is not None, colors_precomp is not None, cov3Ds_precomp is not None)
         ctx.save_for_backward(*[a if a is not None else torch.empty(0) for a in args])
         ctx.mark_non_differentiable(radii)
+        # Outputs the loss does not use (often depth and alpha) arrive as None rather than
+        # as zero tensors, so the backward skips their terms (the gradients are the same).
+        ctx.set_materialize_grads(False)
         return color, radii, depth, alpha
 
     @staticmethod
@@ -263,6 +266,9 @@ class RasterizeGaussiansFn(torch.autograd.Function):
         else:
             scales = rotations = None
         rs = ctx.raster_settings
+        if grad_color is None:
+            grad_color = torch.zeros((3, int(rs.image_height), int(rs.image_width)), dtype=torch.float32,
+                                     device=means3D.device)
         try:
             d_m2, d_col, d_op, d_m3, d_cov, d_sh, d_sc, d_rot = backward(
                 rs, ctx.state, means3D, opac, sh, colors_precomp, scales, rotations, cov3Ds,

@@ -265,3 +265,25 @@ def test_mark_visible(dgr):
     vis = dgr.GaussianRasterizer(rs).markVisible(sc.means3D.to(DEV)).cpu()
     t = torch.cat([sc.means3D, torch.ones(sc.n, 1)], 1) @ sc.camera.viewmatrix[:, 2]
     assert torch.equal(vis, t > 0.2)
+
+
+def test_unused_outputs_give_same_gradients(dgr):
+    """A loss on the colour alone: autograd hands the backward no depth / alpha gradients
+    (None instead of zeros), which must give the same gradient bits as explicit zeros."""
+    from cfgs import raster, scenes
+    sc = scenes.scene_small(n=3000, width=96, height=80, seed=17)
+    rs = settings_for(dgr, sc)
+    s = sc.to(DEV)
+    leaves = [t.clone().requires_grad_(True) for t in (s.means3D, s.opacities, s.shs, s.scales, s.rotations)]
+    m2 = torch.zeros_like(s.means3D, requires_grad=True)
+    color, radii, depth, alpha = dgr.GaussianRasterizer(rs)(means3D=leaves[0], means2D=m2, opacities=leaves[1],
+                                                            shs=leaves[2], scales=leaves[3], rotations=leaves[4])
+    g = l1_image_grad(color, s.target)
+    color.backward(g)
+    c2, r2, d2, a2, st = raster.forward(rs, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None)
+    z = torch.zeros_like(d2)
+    d_m2, d_col, d_op, d_m3, d_cov, d_sh, d_sc, d_rot = raster.backward(
+        rs, st, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None, g, z, z)
+    for got, want in [(leaves[0].grad, d_m3), (leaves[1].grad, d_op), (leaves[2].grad, d_sh), (leaves[3].grad, d_sc),
+                      (leaves[4].grad, d_rot), (m2.grad, d_m2)]:
+        assert torch.equal(got, want)
