@@ -221,6 +221,11 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_preprocess(PreArgs<Scenes>
     campos[0] = sd.campos ? __ldg(sd.campos + 0) : 0.f;
     campos[1] = sd.campos ? __ldg(sd.campos + 1) : 0.f;
     campos[2] = sd.campos ? __ldg(sd.campos + 2) : 0.f;
+    if (a.g.shs) {  // the SH lines are read only after the projection: ask L2 for them now
+      const char* shp = reinterpret_cast<const char*>(a.g.shs + (size_t)idx * sd.sh_coeffs * 3);
+      const int bytes = sd.sh_coeffs * 3 * (int)sizeof(float);
+      for (int o = 0; o < bytes; o += 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(shp + o));
+    }
     float3 p = posed_mean(sd, a.g.means3D, (size_t)idx);
     float3 t = xform43(V, p);
     bool culled = t.z <= CFGS_NEAR_Z;
