@@ -111,7 +111,8 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# algorithmic bytes per launch of each phase
+# algorithmic bytes per launch of each phase: the arrays each phase must read and write
+# once (N Gaussians, K instances, HW pixels, D SH coefficients)
 # ---------------------------------------------------------------------------
 def phase_bytes(N: int, K: int, HW: int, D: int) -> dict:
     params = N * (12 + 4 + 12 * D + 12 + 16)
