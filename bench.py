@@ -42,6 +42,7 @@ def _args():
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-tune", action="store_true", help="keep the default render schedule (no autotuning)")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
     p.add_argument("--workload", default="fwdbwd", choices=["fwdbwd", "pose", "batch", "serve", "ssim", "init", "optim"])
     p.add_argument("--serve-rate", type=float, default=200.0)
@@ -211,8 +212,12 @@ def run_ours(a) -> None:
 
     from cfgs import autotune
     from cfgs.loss import l1_loss_and_grad
-    sched = autotune.tune_rasterizer(rs, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None,
-                                     tuner=autotune.Autotuner())
+    if a.no_tune:
+        sched = autotune.DEFAULT
+        autotune.set_schedule(sched)
+    else:
+        sched = autotune.tune_rasterizer(rs, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None,
+                                         tuner=autotune.Autotuner())
     loss_buf = torch.empty((), dtype=torch.float32, device=dev)
     grad_buf = torch.empty_like(target)
     loss_scratch = torch.empty(4096, dtype=torch.uint8, device=dev)
