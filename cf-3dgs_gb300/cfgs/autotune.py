@@ -86,7 +86,7 @@ def default_cache_path() -> Path:
     return Path.home() / ".cache" / "cfgs" / "autotune.json"
 
 
-def time_cuda(run: Callable[[], None], warmup: int = 2, iters: int = 5) -> float:
+def time_cuda(run: Callable[[], None], warmup: int = 2, iters: int = 10) -> float:
     """Milliseconds per call of run() on the current CUDA stream (events around `iters`
     calls after `warmup` untimed ones)."""
     import torch
@@ -164,7 +164,8 @@ class Autotuner:
         workload, enqueued on the current stream), recorded in the cache. Coordinate
         search: the forward shapes with the default backward batch, then the backward
         batches with the best forward shape. A candidate displaces the incumbent (the
-        default first) only when it is faster by more than `margin`, so timing noise
+        default first) only when it is faster by more than `margin`, and a choice other
+        than the default must win again in an interleaved confirmation, so timing noise
         does not move the choice."""
         if not force:
             hit = self.lookup(key)
@@ -182,6 +183,17 @@ class Autotuner:
         bwd_t = {b: fwd_t[best_fw] if b == DEFAULT.bwd_batch else trial(Schedule(best_fw[0], best_fw[1], b))
                  for b in BWD_CANDIDATES}
         chosen = Schedule(best_fw[0], best_fw[1], pick(BWD_CANDIDATES, bwd_t, margin))
+        if chosen != DEFAULT:
+            # confirmation: both timed twice more, interleaved; the challenger must still win
+            # by the margin on the sum
+            a = b = 0.0
+            for _ in range(2):
+                a += float(self.measure(run, DEFAULT))
+                b += float(self.measure(run, chosen))
+            timings["confirm_default"] = round(a / 2, 5)
+            timings["confirm_chosen"] = round(b / 2, 5)
+            if not b < a * (1.0 - margin):
+                chosen = DEFAULT
         self.record(key, chosen, timings)
         return chosen
 

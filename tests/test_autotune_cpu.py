@@ -62,8 +62,10 @@ def test_tune_coordinate_search_and_cache(tmp_path):
     t = autotune.Autotuner(path, measure=measure)
     s = t.tune("raster/n1/1x1/m1", run=lambda: None)
     assert s == autotune.Schedule(256, 8, 32)
-    # 5 forward shapes at the default backward batch, then 2 more backward batches
-    assert len(calls) == 7 and all(c.bwd_batch == 64 for c in calls[:5])
+    # 5 forward shapes at the default backward batch, 2 more backward batches, then the
+    # interleaved confirmation (default, chosen) x 2
+    assert len(calls) == 11 and all(c.bwd_batch == 64 for c in calls[:5])
+    assert calls[7:] == [autotune.DEFAULT, s, autotune.DEFAULT, s]
     data = json.loads(path.read_text())
     (k, e), = data.items()
     assert k.endswith("|raster/n1/1x1/m1") and e["schedule"] == {"fwd_batch": 256, "fwd_warps": 8, "bwd_batch": 32}
@@ -72,7 +74,22 @@ def test_tune_coordinate_search_and_cache(tmp_path):
     calls.clear()
     t2 = autotune.Autotuner(path, measure=measure)
     assert t2.tune("raster/n1/1x1/m1", run=lambda: None) == s and not calls
-    assert t2.tune("raster/n1/1x1/m1", run=lambda: None, force=True) == s and len(calls) == 7
+    assert t2.tune("raster/n1/1x1/m1", run=lambda: None, force=True) == s and len(calls) == 11
+
+
+def test_confirmation_rejects_a_noisy_winner(tmp_path):
+    from cfgs import autotune
+    seen = {}
+
+    def measure(run, s):  # the 64-batch forward looks fast once, then no longer
+        n = seen.get(s, 0)
+        seen[s] = n + 1
+        if s.fwd_batch == 64 and n == 0:
+            return 9.0
+        return 10.0
+
+    t = autotune.Autotuner(tmp_path / "c.json", measure=measure)
+    assert t.tune("k", run=lambda: None) == autotune.DEFAULT
 
 
 def test_unreadable_cache_is_ignored(tmp_path):
