@@ -211,10 +211,13 @@ template <class Scenes, bool DEPTH, int BATCH>
 __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Scenes> a) {
   static_assert(BATCH % 32 == 0 && BATCH <= kBwdThreads, "whole ballot words, one staged instance per thread");
   constexpr int kBwdBatch = BATCH;
-  __shared__ float4 s_xyt[kBwdBatch];
-  __shared__ float4 s_co[kBwdBatch];
-  __shared__ float4 s_rgbd[kBwdBatch];
-  __shared__ uint32_t s_pidx[kBwdBatch];
+  // Staging buffers come in pairs: batch b - 1 is copied asynchronously (cp.async; its
+  // Gaussian ids were loaded a batch earlier) while batch b is unwound; two block
+  // barriers per batch (staged, then partial sums complete).
+  __shared__ float4 s_xyt[2][kBwdBatch];
+  __shared__ float4 s_co[2][kBwdBatch];
+  __shared__ float4 s_rgbd[2][kBwdBatch];
+  __shared__ uint32_t s_pidx[2][kBwdBatch];
   __shared__ float s_part[kWarps][kBwdBatch][10];
   __shared__ uint32_t s_keep[kWarps][kBwdBatch / 32];
   __shared__ uint32_t s_max;
@@ -246,33 +249,55 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
   __syncthreads();
   const int max_last = (int)s_max;
 
-  const int nb = (max_last + kBwdBatch - 1) / kBwdBatch;
-  for (int b = nb - 1; b >= 0; --b) {
-    const int base = b * kBwdBatch;
-    const int cnt = min(kBwdBatch, max_last - base);
-    __syncthreads();
-    if ((int)threadIdx.x < cnt) {
-      uint32_t i = lo + base + threadIdx.x;
-      uint32_t g = a.sorted_gid[i];
-      s_pidx[threadIdx.x] = a.sorted_pidx[i];
-      float2 m = a.xy[g];
-      float4 co = a.conic_op[g];
-      s_xyt[threadIdx.x] = make_float4(m.x, m.y, alpha_threshold(co.w), 0.0f);
-      s_co[threadIdx.x] = make_float4(-0.5f * co.x, -co.y, -0.5f * co.z, co.w);
-      s_rgbd[threadIdx.x] = a.rgbd[g];
+  const int t = threadIdx.x;
+  auto count_of = [&](int b) { return min(kBwdBatch, max_last - b * kBwdBatch); };
+  uint32_t gnext = 0;
+  auto load_id = [&](int b) { gnext = t < count_of(b) ? a.sorted_gid[lo + b * kBwdBatch + t] : 0u; };
+  auto issue = [&](int b, int buf) {
+    if (t < count_of(b)) {
+      const uint32_t i = lo + (uint32_t)(b * kBwdBatch + t);
+      cp_async4(&s_pidx[buf][t], a.sorted_pidx + i);
+      cp_async8(&s_xyt[buf][t], a.xy + gnext);
+      cp_async16(&s_co[buf][t], a.conic_op + gnext);
+      cp_async16(&s_rgbd[buf][t], a.rgbd + gnext);
     }
-    __syncthreads();
+    cp_async_commit();
+  };
+  const int nb = (max_last + kBwdBatch - 1) / kBwdBatch;
+  if (nb > 0) {
+    load_id(nb - 1);
+    issue(nb - 1, 0);
+    if (nb > 1) load_id(nb - 2);
+  }
+  for (int k = 0; k < nb; ++k) {
+    const int b = nb - 1 - k, cur = k & 1;
+    const int base = b * kBwdBatch;
+    const int cnt = count_of(b);
+    cp_async_wait_all();
+    if (t < cnt) {  // raw (x, y) and conic -> render form, own slot
+      const float4 co = s_co[cur][t];
+      s_xyt[cur][t].z = alpha_threshold(co.w);
+      s_co[cur][t] = make_float4(-0.5f * co.x, -co.y, -0.5f * co.z, co.w);
+    }
+    __syncthreads();  // batch b staged; batch b + 1 finished, so its buffers are free
+    if (b > 0) {
+      issue(b - 1, cur ^ 1);
+      if (b > 1) load_id(b - 2);
+    }
+    const float4* s_xyt_b = s_xyt[cur];
+    const float4* s_co_b = s_co[cur];
+    const float4* s_rgbd_b = s_rgbd[cur];
     uint32_t keep[kBwdBatch / 32];
 #pragma unroll
     for (int r = 0; r < kBwdBatch / 32; ++r) {
       const int j = r * 32 + lane;
-      bool k = false;
+      bool kp = false;
       if (j < cnt && base + j < warp_last) {
-        const float4 xyt = s_xyt[j];
-        const float4 co = s_co[j];
-        k = box_may_contribute(make_float2(xyt.x, xyt.y), co.x, co.y, co.z, xyt.z, bxf0, bxf1, byf0, byf1);
+        const float4 xyt = s_xyt_b[j];
+        const float4 co = s_co_b[j];
+        kp = box_may_contribute(make_float2(xyt.x, xyt.y), co.x, co.y, co.z, xyt.z, bxf0, bxf1, byf0, byf1);
       }
-      keep[r] = __ballot_sync(0xffffffffu, k);
+      keep[r] = __ballot_sync(0xffffffffu, kp);
       if (lane == 0) s_keep[warp][r] = keep[r];
     }
 #pragma unroll
@@ -285,10 +310,10 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
         const int c = base + j;
         float v[10];
 #pragma unroll
-        for (int k = 0; k < 10; ++k) v[k] = 0.f;
-        const float4 m = s_xyt[j];
-        const float4 co = s_co[j];
-        const bool contrib = unwind_pair<DEPTH>(pp, c, pxf, pyf, m, co, s_rgbd, j, v);
+        for (int q = 0; q < 10; ++q) v[q] = 0.f;
+        const float4 m = s_xyt_b[j];
+        const float4 co = s_co_b[j];
+        const bool contrib = unwind_pair<DEPTH>(pp, c, pxf, pyf, m, co, s_rgbd_b, j, v);
         if (__ballot_sync(0xffffffffu, contrib)) {
           warp_reduce_terms<DEPTH>(v, lane);
           if ((lane & 3) == 0) s_part[warp][j][lane >> 2] = v[0];
@@ -301,18 +326,18 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
         }
       }
     }
-    __syncthreads();
-    if ((int)threadIdx.x < cnt) {
-      const int j = threadIdx.x;
+    __syncthreads();  // every warp's partial sums of batch b are in
+    if (t < cnt) {
+      const int j = t;
       float sum[10];
 #pragma unroll
-      for (int k = 0; k < 10; ++k) sum[k] = 0.f;
+      for (int q = 0; q < 10; ++q) sum[q] = 0.f;
 #pragma unroll
       for (int w = 0; w < kWarps; ++w)
         if ((s_keep[w][j >> 5] >> (j & 31)) & 1u)
 #pragma unroll
-          for (int k = 0; k < 10; ++k) sum[k] += s_part[w][j][k];
-      finish_record(a.records + (size_t)kRecordFloat4 * s_pidx[threadIdx.x], sum, s_co[j]);
+          for (int q = 0; q < 10; ++q) sum[q] += s_part[w][j][q];
+      finish_record(a.records + (size_t)kRecordFloat4 * s_pidx[cur][j], sum, s_co_b[j]);
     }
   }
   for (int i = max_last + threadIdx.x; i < n; i += blockDim.x) {
