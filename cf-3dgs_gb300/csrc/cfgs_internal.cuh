@@ -42,7 +42,7 @@ inline bool ensure_dynamic_smem(Kernel* kernel, int bytes, std::atomic<uint64_t>
 // elements: kDepthChunk for the depth sort of the Gaussians (4 passes), kTileChunk for
 // the tile sort of the instances.
 constexpr int kDepthChunk = 1024;
-constexpr int kTileChunk = 2048;
+constexpr int kTileChunk = 1024;
 constexpr int kSortDigits = 256;  // digits per pass at most (8 bits)
 constexpr int kDepthPasses = 4;
 constexpr int kMaxTilePasses = 4;
