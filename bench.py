@@ -166,10 +166,10 @@ def _peaks() -> dict:
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
-# capture of the 1M-Gaussian 1080p workload (profiles/traffic_1M_1080p.md), at the
+# capture of the 1M-Gaussian 1080p workload (profiles/launches_fwd_bwd_1M_1080p.md), at the
 # instance count K it was taken at; scaled by instances for another K.
-NCU_TRAFFIC = {"render_bwd": (362095616 + 673941760, 12433348),
-               "composite": (66856960 + 28301824, 12433348)}
+NCU_TRAFFIC = {"render_bwd": (377723392 + 682768128, 12433348),
+               "composite": (66645248 + 27697152, 12433348)}
 
 
 def _traffic(kernel: str, K: int):
