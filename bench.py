@@ -31,6 +31,24 @@ METRIC = "fwd+bwd iters/s at 1M Gaussians 1080p"
 UNIT = "iters/s"
 
 
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The largest of the ranks' values (the slowest rank's time); x itself for one rank.
+    Every rank must call it (a collective on the default process group)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world: int, steps: int, seconds: float) -> float:
+    """Whole-job throughput: every rank runs `steps` units; the job takes the slowest
+    rank's time."""
+    return world * steps / seconds
+
+
 def _args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -250,13 +268,9 @@ def run_ours(a) -> None:
     t1.record()
     barrier()
     clk = clocks.stop()
-    total_ms = t0.elapsed_time(t1)
-    if world > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(t0.elapsed_time(t1), world, dev)
     ms_per_step = total_ms / a.steps
-    value = world * a.steps / (total_ms / 1000.0)
+    value = job_rate(world, a.steps, total_ms / 1000.0)
 
     phase_ms = {k: sum(s_.elapsed_time(e_) for s_, e_ in v) / len(v) for k, v in timers.items()}
     D = (sc.sh_degree + 1) ** 2
@@ -388,22 +402,16 @@ def run_e2e(a, dgr, sc, rs, dev, barrier, world) -> dict:
         t0 = time.perf_counter()
         fn()
         barrier()
-        dt = time.perf_counter() - t0
-        if world > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([dt], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            dt = float(tt.item())
-        return dt
+        return max_over_ranks(time.perf_counter() - t0, world, dev)
 
     dt_serial = timed(lambda: [serial_step() for _ in range(steps)])
     dt = timed(lambda: run_pipelined(steps))
-    return {"value": round(world * steps / dt, 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+    return {"value": round(job_rate(world, steps, dt), 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": 4, "steps": steps, "api": "diff_gaussian_rasterization.GaussianRasterizer",
             "copies": "next step's inputs on a second stream during the current step",
             "loss_read": "every step's loss copied to pinned host memory and read after the next step is enqueued",
             "ms_per_step": round(dt * 1000.0 / steps, 4),
-            "serial": {"value": round(world * steps / dt_serial, 4), "ms_per_step": round(dt_serial * 1000.0 / steps, 4)},
+            "serial": {"value": round(job_rate(world, steps, dt_serial), 4), "ms_per_step": round(dt_serial * 1000.0 / steps, 4)},
             "h2d_ms_alone": round(h2d_ms, 4), "h2d_gb_per_s": round(h2d / (h2d_ms / 1000.0) / 1e9, 1)}
 
 
@@ -460,7 +468,7 @@ def run_reference(a) -> None:
     value = steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": a.gpus,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1000 * dt / a.steps, 2), "higher_is_better": True,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1000 * dt / steps, 2), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{sc.n} SH{sc.sh_degree} Gaussians, {a.width}x{a.height}, fwd + L1 loss + bwd"},
         "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": cores, "kind": "port",
