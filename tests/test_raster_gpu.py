@@ -287,3 +287,29 @@ def test_unused_outputs_give_same_gradients(dgr):
     for got, want in [(leaves[0].grad, d_m3), (leaves[1].grad, d_op), (leaves[2].grad, d_sh), (leaves[3].grad, d_sc),
                       (leaves[4].grad, d_rot), (m2.grad, d_m2)]:
         assert torch.equal(got, want)
+
+
+def test_split_binning_equals_one_call(dgr):
+    """cfgs_depth_order + cfgs_bin_instances (the drop-in forward's split, which lets the
+    depth sort run while the host reads K) leave the same workspaces as cfgs_bin_forward."""
+    import ctypes as C
+    from cfgs import native, raster, scenes
+    sc = scenes.scene_small(n=5000, width=160, height=120, seed=23)
+    rs = settings_for(dgr, sc)
+    s = sc.to(DEV)
+    color, radii, depth, alpha, st = raster.forward(rs, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations,
+                                                    None)
+    ref = raster.inspect_state(st, sc.camera.width, sc.camera.height)
+    lib = native.load()
+    keep: list = []
+    cs = raster.make_settings(rs, keep)
+    g = raster.make_gaussians(s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None)
+    binning = torch.zeros_like(st.binning)
+    native.check(lib.cfgs_bin_forward(C.byref(cs), C.byref(g), st.geom.data_ptr(), st.image.data_ptr(),
+                                      binning.data_ptr(), st.num_rendered, raster.stream_handle(s.means3D.device)),
+                 "cfgs_bin_forward")
+    torch.cuda.synchronize()
+    got = raster.inspect_state(raster.ForwardState(st.geom, st.image, binning, st.num_rendered, st.radii),
+                               sc.camera.width, sc.camera.height)
+    for k in ("sorted_gid", "sorted_pidx", "tile_range", "offset"):
+        assert torch.equal(got[k], ref[k]), k
