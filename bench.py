@@ -62,7 +62,8 @@ def _args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-tune", action="store_true", help="keep the default render schedule (no autotuning)")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
-    p.add_argument("--workload", default="fwdbwd", choices=["fwdbwd", "pose", "batch", "serve", "ssim", "init", "optim"])
+    p.add_argument("--workload", default="fwdbwd",
+                   choices=["fwdbwd", "pose", "pose_iter", "batch", "serve", "ssim", "init", "optim"])
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--serve-seconds", type=float, default=60.0)
     p.add_argument("--serve-slots", type=int, default=64)
@@ -546,6 +547,40 @@ def run_pose(a) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_pose_iter(a) -> None:
+    """One iteration of the solve engine on the 640x360 pose problem, eager launches (no
+    graph): W untimed iterations, then K timed with CUDA events; a small, fixed sequence
+    of launches for profilers."""
+    import ctypes as C
+    import torch
+    import diff_gaussian_rasterization  # noqa: F401
+    from cfgs import batch, native, pose, scenes
+    dev = torch.device("cuda", 0)
+    prob = pose.make_problem(scenes.scene_pose(width=640, height=360, seed=2), dev)
+    bs = batch.BatchSolver([prob])
+    K0 = bs.probe_capacity()
+    bs.reset()
+    bs._alloc_instances(int(K0 * bs.capacity_factor) + 4096)
+    args = bs._args()
+    st = torch.cuda.current_stream(dev).cuda_stream
+    native.check(bs.lib.cfgs_batch_init(C.byref(args), st), "cfgs_batch_init")
+    for _ in range(a.warmup):
+        native.check(bs.lib.cfgs_batch_iteration(C.byref(args), st), "cfgs_batch_iteration")
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record()
+    for _ in range(a.steps):
+        native.check(bs.lib.cfgs_batch_iteration(C.byref(args), st), "cfgs_batch_iteration")
+    t1.record()
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / max(a.steps, 1)
+    print(json.dumps({"metric": "pose-solve engine iteration (640x360, eager launches)", "value": round(ms, 4),
+                      "unit": "ms/iteration", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+                      "higher_is_better": False, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": "CF-3DGS relative pose solve, 230400 SH0 Gaussians, 640x360",
+                                 "num_rendered": int(K0)}}), flush=True)
+
+
 def run_batch(a) -> None:
     """64 pose solves (N log-uniform in [5e4, 5e5], resolutions 320x180/640x360/960x540)
     batched in one launch per stage with CUDA-graph replays, vs the same solves one by one
@@ -858,6 +893,8 @@ def main():
         run_reference(a)
     elif a.workload == "pose":
         run_pose(a)
+    elif a.workload == "pose_iter":
+        run_pose_iter(a)
     elif a.workload == "batch":
         run_batch(a)
     elif a.workload == "serve":
