@@ -551,26 +551,21 @@ def run_pose_iter(a) -> None:
     """One iteration of the solve engine on the 640x360 pose problem, eager launches (no
     graph): W untimed iterations, then K timed with CUDA events; a small, fixed sequence
     of launches for profilers."""
-    import ctypes as C
     import torch
     import diff_gaussian_rasterization  # noqa: F401
-    from cfgs import batch, native, pose, scenes
+    from cfgs import batch, pose, scenes
     dev = torch.device("cuda", 0)
     prob = pose.make_problem(scenes.scene_pose(width=640, height=360, seed=2), dev)
     bs = batch.BatchSolver([prob])
-    K0 = bs.probe_capacity()
-    bs.reset()
-    bs._alloc_instances(int(K0 * bs.capacity_factor) + 4096)
-    args = bs._args()
-    st = torch.cuda.current_stream(dev).cuda_stream
-    native.check(bs.lib.cfgs_batch_init(C.byref(args), st), "cfgs_batch_init")
+    args = bs.prepare()
+    K0 = bs.capacity
     for _ in range(a.warmup):
-        native.check(bs.lib.cfgs_batch_iteration(C.byref(args), st), "cfgs_batch_iteration")
+        bs.iterate(args)
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     t0.record()
     for _ in range(a.steps):
-        native.check(bs.lib.cfgs_batch_iteration(C.byref(args), st), "cfgs_batch_iteration")
+        bs.iterate(args)
     t1.record()
     torch.cuda.synchronize()
     ms = t0.elapsed_time(t1) / max(a.steps, 1)
@@ -578,7 +573,7 @@ def run_pose_iter(a) -> None:
                       "unit": "ms/iteration", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
                       "higher_is_better": False, "dtype": "f32", "data": "synthetic",
                       "config": {"workload": "CF-3DGS relative pose solve, 230400 SH0 Gaussians, 640x360",
-                                 "num_rendered": int(K0)}}), flush=True)
+                                 "instance_capacity": int(K0)}}), flush=True)
 
 
 def run_batch(a) -> None:

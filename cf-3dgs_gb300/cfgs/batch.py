@@ -233,6 +233,22 @@ class BatchSolver:
         return False
 
     # ---- running -------------------------------------------------------------------
+    def prepare(self) -> native.BatchArgs:
+        """Resets every solve, sizes the instance capacity from a counting iteration and
+        initialises the pose states; returns the arguments for iterate()."""
+        K0 = self.probe_capacity()
+        self.reset()
+        self._alloc_instances(int(K0 * self.capacity_factor) + 4096)
+        args = self._args()
+        native.check(self.lib.cfgs_batch_init(C.byref(args), torch.cuda.current_stream(self.dev).cuda_stream),
+                     "cfgs_batch_init")
+        return args
+
+    def iterate(self, args: native.BatchArgs) -> None:
+        """Enqueues one iteration of every solve (eager launches, no graph)."""
+        native.check(self.lib.cfgs_batch_iteration(C.byref(args), torch.cuda.current_stream(self.dev).cuda_stream),
+                     "cfgs_batch_iteration")
+
     def probe_capacity(self) -> int:
         """K of the current poses (an iteration at capacity 0 only counts; the update
         is skipped), and a capacity with headroom for the poses to move."""

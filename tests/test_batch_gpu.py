@@ -76,3 +76,16 @@ def test_batch_solve_recovers_pose(mods):
         e0 = pose.pose_error(np.zeros(6), p.xi_gt)
         e1 = pose.pose_error(res.xi[s], p.xi_gt)
         assert e1[0] < 0.25 * e0[0] + 0.01 and e1[1] < 0.25 * e0[1] + 1e-3, (s, e0, e1)
+
+
+def test_prepare_and_iterate_equal_solve(mods):
+    """The eager interface (prepare() + iterate()) takes the same steps as solve()."""
+    batch, pose, scenes = mods
+    probs = _problems(pose, scenes, SPECS[:2])
+    ref = batch.BatchSolver(probs, use_graph=False).solve(15).xi
+    bs = batch.BatchSolver(probs, use_graph=False)
+    args = bs.prepare()
+    for _ in range(15):
+        bs.iterate(args)
+    torch.cuda.synchronize()
+    assert np.array_equal(bs.xi.double().cpu().numpy(), ref)
