@@ -122,3 +122,34 @@ def test_oracle_exp_accuracy():
     assert worst <= 2.0, worst
     assert c_oracle.exp(-200.0) == 0.0
     assert math.isinf(c_oracle.exp(100.0))
+
+
+@pytest.mark.parametrize("seed,n,w,h", [(3, 2000, 100, 75), (4, 500, 33, 17)])
+def test_c_oracle_keys_and_ranges_are_a_stable_sort(seed, n, w, h):
+    """The oracle's binning is the published one: every (Gaussian, touched tile) pair in
+    Gaussian order with the 64-bit key tile << 32 | depth bits, stably sorted by key; the
+    tile ranges are the key boundaries. Rebuilt here in numpy from the oracle's own
+    per-Gaussian outputs (rectangles, depths)."""
+    from cfgs import scenes
+    from oracle.c_oracle import Oracle
+    sc = scenes.scene_small(n=n, width=w, height=h, seed=seed)
+    o = Oracle.from_scene(sc).forward()
+    keys, gids = [], []
+    for g in range(n):
+        if o.radii[g] <= 0:
+            continue
+        x0, y0, x1, y1 = (int(v) for v in o.rect[g])
+        dbits = int(np.float32(o.rgbd[g, 3]).view(np.uint32))
+        for ty in range(y0, y1):
+            for tx in range(x0, x1):
+                keys.append(((ty * o.gx + tx) << 32) | dbits)
+                gids.append(g)
+    keys = np.array(keys, dtype=np.uint64)
+    gids = np.array(gids, dtype=np.uint32)
+    order = np.argsort(keys, kind="stable")
+    assert o.K == len(keys)
+    np.testing.assert_array_equal(o.keys, keys[order])
+    np.testing.assert_array_equal(o.gid, gids[order])
+    tiles = (keys[order] >> np.uint64(32)).astype(np.int64)
+    want = np.searchsorted(tiles, np.arange(o.gx * o.gy + 1), side="left")
+    np.testing.assert_array_equal(o.ranges.astype(np.int64), want)
