@@ -153,3 +153,30 @@ def test_c_oracle_keys_and_ranges_are_a_stable_sort(seed, n, w, h):
     tiles = (keys[order] >> np.uint64(32)).astype(np.int64)
     want = np.searchsorted(tiles, np.arange(o.gx * o.gy + 1), side="left")
     np.testing.assert_array_equal(o.ranges.astype(np.int64), want)
+
+
+def test_c_oracle_edge_scenes():
+    """Empty input, every Gaussian behind the camera, and screen-filling Gaussians: the
+    C oracle against the float64 restatement."""
+    from cfgs import scenes
+    from oracle.c_oracle import Oracle
+    empty = scenes.scene_small(n=0, width=33, height=17, seed=1)
+    o = Oracle.from_scene(empty).forward()
+    assert o.K == 0 and np.all(o.n_contrib == 0) and np.all(o.final_T == 1.0)
+    np.testing.assert_array_equal(o.color, np.broadcast_to(empty.bg.numpy()[:, None, None], o.color.shape))
+
+    behind = scenes.scene_small(n=200, width=48, height=40, seed=2)
+    m = behind.means3D.clone()
+    m[:, 2] = -m[:, 2].abs() - 1.0          # every centre behind the camera
+    behind.means3D = m
+    o = Oracle.from_scene(behind).forward()
+    assert o.K == 0 and np.all(o.radii == 0)
+
+    big = scenes.scene_small(n=300, width=64, height=48, seed=3)
+    s = big.scales.clone()
+    s[:4] = 0.8                              # a few Gaussians that cover every tile
+    big.scales = s
+    o, r, _, _ = _both(big)
+    assert o.K >= 4 * o.gx * o.gy
+    np.testing.assert_array_equal(r["radii"].numpy(), o.radii)
+    assert np.abs(r["color"].detach().numpy() - o.color).max() <= 1e-5
