@@ -53,7 +53,7 @@ def lib():
         L.oracle_render.argtypes = [C.POINTER(OSettings), C.POINTER(OGeom), _u32p, _u32p, _fp, _fp, _fp, _fp, _u32p]
         L.oracle_render_backward.restype = None
         L.oracle_render_backward.argtypes = [C.POINTER(OSettings), C.c_int, C.POINTER(OGeom), _u32p, _u32p, _fp,
-                                             _u32p, _fp, _fp, _fp, _dp]
+                                             _u32p, _fp, _fp, _fp, _dp, _dp]
         L.oracle_preprocess_backward.restype = None
         L.oracle_preprocess_backward.argtypes = [C.POINTER(OSettings), C.POINTER(OGauss), C.POINTER(OGeom), _dp,
                                                  _fp, _fp, _fp, _fp, _fp, _fp, _fp, _fp]
@@ -151,18 +151,31 @@ class Oracle:
         self.gid = self.gid[:K]
         return self
 
-    def backward(self, dL_dcolor, dL_ddepth=None, dL_dalpha=None):
+    def backward(self, dL_dcolor, dL_ddepth=None, dL_dalpha=None, magnitudes=False):
+        """Gradients of every input (float64 sums rounded to float32 at the end). With
+        magnitudes=True it also keeps, per Gaussian, the magnitudes of the per-pixel terms
+        behind its ten 2D gradient sums (self.g10abs [N,20]: the sums of their absolute
+        values, then the same weighted by the contributions unwound before each), which
+        oracle.error_bound turns into per-element float32 rounding bounds."""
         L = lib()
         N, M = self.N, self.M
         dc = _np(dL_dcolor).reshape(-1)
         dd = _np(dL_ddepth).reshape(-1) if dL_ddepth is not None else None
         da = _np(dL_dalpha).reshape(-1) if dL_dalpha is not None else None
         g10 = np.zeros((max(N, 1), 10), np.float64)
+        g10abs = np.zeros((max(N, 1), 20), np.float64) if magnitudes else None
         gid = self.gid if self.K > 0 else np.zeros(1, np.uint32)
         L.oracle_render_backward(C.byref(self.s), N, C.byref(self.geom), _p(gid, _u32p), _p(self.ranges, _u32p),
                                  _p(self.final_T, _fp), _p(self.n_contrib, _u32p), _p(dc, _fp), _p(dd, _fp),
-                                 _p(da, _fp), _p(g10, _dp))
+                                 _p(da, _fp), _p(g10, _dp), _p(g10abs, _dp))
         self.g10 = g10[:N]
+        self.g10abs = None if g10abs is None else g10abs[:N]
+        return self._preprocess_backward(g10)
+
+    def _preprocess_backward(self, g10):
+        L = lib()
+        N, M = self.N, self.M
+        g10 = np.ascontiguousarray(g10, np.float64)
         out = {
             "means2D": np.zeros((N, 3), np.float32),
             "colors": np.zeros((N, 3), np.float32),

@@ -458,11 +458,12 @@ void oracle_render(const OSettings* s, const OGeom* o, const uint32_t* gid, cons
  * drgb (3), ddepth — accumulated in double into g10 [N,10]. */
 void oracle_render_backward(const OSettings* s, int N, const OGeom* o, const uint32_t* gid, const uint32_t* ranges,
                             const float* final_T, const uint32_t* n_contrib, const float* dL_dcolor,
-                            const float* dL_ddepth, const float* dL_dalpha, double* g10) {
+                            const float* dL_ddepth, const float* dL_dalpha, double* g10, double* g10abs) {
   const int gx = (s->W + TILE - 1) / TILE, gy = (s->H + TILE - 1) / TILE;
   const size_t HW = (size_t)s->W * s->H;
   const int64_t K = ranges[gx * gy];
   double* part = (double*)calloc((size_t)(K > 0 ? K : 1) * 10, sizeof(double));
+  double* pabs = g10abs ? (double*)calloc((size_t)(K > 0 ? K : 1) * 20, sizeof(double)) : NULL;
 #pragma omp parallel for schedule(dynamic, 4)
   for (int tile = 0; tile < gx * gy; ++tile) {
     const int tx = tile % gx, ty = tile / gx;
@@ -479,6 +480,7 @@ void oracle_render_backward(const OSettings* s, int N, const OGeom* o, const uin
         const double bg_dot = s->bg[0] * dC[0] + s->bg[1] * dC[1] + s->bg[2] * dC[2];
         double T = Tf;
         double acc[4] = {0, 0, 0, 0}, lastc[4] = {0, 0, 0, 0}, last_a = 0.0;
+        double unwound = 0.0; /* contributions of this pixel already unwound (back to front) */
         uint32_t last = n_contrib[pix];
         for (int64_t c = (int64_t)last - 1; c >= 0; --c) {
           uint32_t i = ranges[tile] + (uint32_t)c;
@@ -500,6 +502,7 @@ void oracle_render_backward(const OSettings* s, int N, const OGeom* o, const uin
           double w = alpha * T;
           double col[4] = {o->rgbd[4 * g], o->rgbd[4 * g + 1], o->rgbd[4 * g + 2], o->rgbd[4 * g + 3]};
           double* pp = part + (size_t)i * 10;
+          double* pa = pabs ? pabs + (size_t)i * 20 : NULL;
           pp[6] += dC[0] * w;
           pp[7] += dC[1] * w;
           pp[8] += dC[2] * w;
@@ -521,12 +524,47 @@ void oracle_render_backward(const OSettings* s, int N, const OGeom* o, const uin
           pp[2] += -0.5 * dx * dx * dp;
           pp[3] += -dx * dy * dp;
           pp[4] += -0.5 * dy * dy * dp;
+          if (pa) {
+            /* Magnitudes of what each sum adds up: the same terms with every product and
+               sum of products taken in absolute value (pa[0..9]), and the same weighted by
+               the number of contributions of the pixel unwound before this one
+               (pa[10..19]). A float32 evaluation of the sums, in any order, rounds on the
+               scale of the first; the transmittance and the colour behind, rebuilt back to
+               front one contribution at a time, carry a rounding per step, on the scale
+               of the second. */
+            const double adLda = (fabs(col[0]) + fabs(acc[0])) * fabs(dC[0]) + (fabs(col[1]) + fabs(acc[1])) * fabs(dC[1]) +
+                                 (fabs(col[2]) + fabs(acc[2])) * fabs(dC[2]) + (fabs(col[3]) + fabs(acc[3])) * fabs(dD);
+            const double aL = adLda * T + Tf / (1.0 - alpha) * (fabs(dA) + fabs(bg_dot));
+            const double adp = G * op * aL;
+            double t10[10];
+            t10[0] = adp * (2.0 * fabs(ca * dx) + fabs(cb * dy));
+            t10[1] = adp * (2.0 * fabs(cc * dy) + fabs(cb * dx));
+            t10[2] = 0.5 * dx * dx * adp;
+            t10[3] = fabs(dx * dy) * adp;
+            t10[4] = 0.5 * dy * dy * adp;
+            t10[5] = G * aL;
+            t10[6] = fabs(dC[0]) * w;
+            t10[7] = fabs(dC[1]) * w;
+            t10[8] = fabs(dC[2]) * w;
+            t10[9] = fabs(dD) * w;
+            for (int k = 0; k < 10; ++k) {
+              pa[k] += t10[k];
+              pa[10 + k] += unwound * t10[k];
+            }
+          }
+          unwound += 1.0;
         }
       }
   }
   memset(g10, 0, sizeof(double) * 10 * (size_t)N);
   for (int64_t i = 0; i < K; ++i)
     for (int k = 0; k < 10; ++k) g10[(size_t)gid[i] * 10 + k] += part[(size_t)i * 10 + k];
+  if (pabs) {
+    memset(g10abs, 0, sizeof(double) * 20 * (size_t)N);
+    for (int64_t i = 0; i < K; ++i)
+      for (int k = 0; k < 20; ++k) g10abs[(size_t)gid[i] * 20 + k] += pabs[(size_t)i * 20 + k];
+    free(pabs);
+  }
   free(part);
 }
 
@@ -615,9 +653,9 @@ void oracle_preprocess_backward(const OSettings* s, const OGauss* g, const OGeom
     const double cc = T1[0] * v[0] + T1[1] * v[1] + T1[2] * v[2] + 0.3;
     const double dA = a[2], dB = a[3], dC = a[4];
     const double det = ca * cc - cb * cb, id = 1.0 / det, id2 = id * id;
-    const double da = dA * (-cc * cc * id2) + dB * (cb * cc * id2) + dC * (id - ca * cc * id2);
+    const double da = dA * (-cc * cc * id2) + dB * (cb * cc * id2) + dC * (-cb * cb * id2);
     const double db = dA * (2 * cb * cc * id2) + dB * (-id - 2 * cb * cb * id2) + dC * (2 * ca * cb * id2);
-    const double dc = dA * (id - ca * cc * id2) + dB * (ca * cb * id2) + dC * (-ca * ca * id2);
+    const double dc = dA * (-cb * cb * id2) + dB * (ca * cb * id2) + dC * (-ca * ca * id2);
     double dcov[6];
     dcov[0] = da * T0[0] * T0[0] + db * T0[0] * T1[0] + dc * T1[0] * T1[0];
     dcov[3] = da * T0[1] * T0[1] + db * T0[1] * T1[1] + dc * T1[1] * T1[1];

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import assert_grad_close, bits, l1_image_grad, settings_for
+from helpers import assert_grad_bounded, bits, l1_image_grad, settings_for
 
 pytestmark = pytest.mark.gpu
 
@@ -143,14 +143,13 @@ def test_backward_matches_oracle(dgr, case):
         sc = _dense_scene()
     color, radii, depth, alpha, leaves, (gc, gd, ga) = _run_autograd(dgr, sc)
     from oracle.c_oracle import Oracle
+    from oracle.error_bound import backward_bounds
     ref = Oracle.from_scene(sc).forward()
-    want = ref.backward(gc.numpy(), gd.numpy(), ga.numpy())
-    assert_grad_close("means2D", leaves["means2D"].grad.cpu(), want["means2D"])
-    assert_grad_close("opacities", leaves["opacities"].grad.cpu(), want["opacity"])
-    assert_grad_close("means3D", leaves["means3D"].grad.cpu(), want["means3D"])
-    assert_grad_close("shs", leaves["shs"].grad.cpu(), want["sh"])
-    assert_grad_close("scales", leaves["scales"].grad.cpu(), want["scales"])
-    assert_grad_close("rotations", leaves["rotations"].grad.cpu(), want["rotations"])
+    want = ref.backward(gc.numpy(), gd.numpy(), ga.numpy(), magnitudes=True)
+    bound = backward_bounds(ref)
+    for leaf, key in (("means2D", "means2D"), ("opacities", "opacity"), ("means3D", "means3D"), ("shs", "sh"),
+                      ("scales", "scales"), ("rotations", "rotations")):
+        assert_grad_bounded(leaf, leaves[leaf].grad.cpu(), want[key], bound[key])
 
 
 def test_backward_matches_torch_autograd(dgr):
@@ -171,12 +170,19 @@ def test_backward_matches_torch_autograd(dgr):
     np.testing.assert_array_equal(r["radii"].numpy(), radii.cpu().numpy())
     L = (r["color"] * gc.double()).sum() + (r["depth"] * gd.double()).sum() + (r["alpha"] * ga.double()).sum()
     L.backward()
-    assert_grad_close("means2D", leaves["means2D"].grad.cpu(), m2.grad, floor=0.1)
-    assert_grad_close("means3D", leaves["means3D"].grad.cpu(), ref["means3D"].grad, floor=0.1)
-    assert_grad_close("opacities", leaves["opacities"].grad.cpu(), ref["opacities"].grad, floor=0.1)
-    assert_grad_close("shs", leaves["shs"].grad.cpu(), ref["shs"].grad, floor=0.1)
-    assert_grad_close("scales", leaves["scales"].grad.cpu(), ref["scales"].grad, floor=0.1)
-    assert_grad_close("rotations", leaves["rotations"].grad.cpu(), ref["rotations"].grad, floor=0.1)
+    # the float32 rounding bound of the kernels' computation on this scene (the dense
+    # float64 restatement is exact to far below it)
+    from oracle.c_oracle import Oracle
+    from oracle.error_bound import backward_bounds
+    co = Oracle.from_scene(sc).forward()
+    co.backward(gc.numpy(), gd.numpy(), ga.numpy(), magnitudes=True)
+    bound = backward_bounds(co)
+    assert_grad_bounded("means2D", leaves["means2D"].grad.cpu(), m2.grad, bound["means2D"])
+    assert_grad_bounded("means3D", leaves["means3D"].grad.cpu(), ref["means3D"].grad, bound["means3D"])
+    assert_grad_bounded("opacities", leaves["opacities"].grad.cpu(), ref["opacities"].grad, bound["opacity"])
+    assert_grad_bounded("shs", leaves["shs"].grad.cpu(), ref["shs"].grad, bound["sh"])
+    assert_grad_bounded("scales", leaves["scales"].grad.cpu(), ref["scales"].grad, bound["scales"])
+    assert_grad_bounded("rotations", leaves["rotations"].grad.cpu(), ref["rotations"].grad, bound["rotations"])
 
 
 def test_precomputed_inputs_match(dgr):
@@ -217,10 +223,12 @@ def test_precomputed_backward_matches_oracle(dgr):
                                                                      colors=colors, cov=cov)
     ref = Oracle.from_scene(sc, use_colors=True, colors=colors, use_cov=True, cov=cov).forward()
     np.testing.assert_array_equal(bits(color.detach().cpu().numpy()), bits(ref.color))
-    want = ref.backward(gc.numpy(), gd.numpy(), ga.numpy())
-    assert_grad_close("colors_precomp", leaves["colors_precomp"].grad.cpu(), want["colors"])
-    assert_grad_close("cov3D_precomp", leaves["cov3D_precomp"].grad.cpu(), want["cov3D"])
-    assert_grad_close("means3D", leaves["means3D"].grad.cpu(), want["means3D"])
+    want = ref.backward(gc.numpy(), gd.numpy(), ga.numpy(), magnitudes=True)
+    from oracle.error_bound import backward_bounds
+    bound = backward_bounds(ref)
+    assert_grad_bounded("colors_precomp", leaves["colors_precomp"].grad.cpu(), want["colors"], bound["colors"])
+    assert_grad_bounded("cov3D_precomp", leaves["cov3D_precomp"].grad.cpu(), want["cov3D"], bound["cov3D"])
+    assert_grad_bounded("means3D", leaves["means3D"].grad.cpu(), want["means3D"], bound["means3D"])
 
 
 def test_empty_and_culled(dgr):
