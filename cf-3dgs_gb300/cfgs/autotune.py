@@ -1,6 +1,7 @@
 """Render-schedule autotuner.
 
-The two per-tile render kernels have several launch shapes (cfgs_set_render_schedule):
+The two per-tile render kernels have several launch shapes (CfgsRenderSchedule, a
+field of every call's settings):
 the forward's staging batch and warps per tile (4 warps on 8x8 pixel boxes with two
 pixels per lane, or 8 warps on 8x4 boxes with one), and the backward's staging batch.
 Every shape gives bit-identical results, so the choice only changes speed: the 4-warp
@@ -12,12 +13,17 @@ The tuner times the candidates on the caller's own workload with CUDA events and
 the winner in a JSON cache keyed by the workload's shape — the Gaussian count rounded
 up to a power of two, the image size (or, for a batch of solves, the tile count rounded
 up to a power of two) and the SH width — so a shape is tuned once per cache.
+
+The library keeps no schedule: each call carries one. On the host side the schedule
+calls use is the calling thread's current one (set_schedule / using), so threads that
+render different workloads with different schedules do not affect each other.
 """
 from __future__ import annotations
 
 import json
 import os
 import tempfile
+import threading
 from contextlib import contextmanager
 from dataclasses import asdict, dataclass
 from pathlib import Path
@@ -38,23 +44,31 @@ FWD_CANDIDATES = [(128, 4), (64, 4), (256, 4), (128, 8), (256, 8)]  # (fwd_batch
 BWD_CANDIDATES = [64, 32, 128]
 
 
+_thread = threading.local()
+
+
+def c_schedule(s: Schedule | None = None) -> "native.RenderSchedule":
+    """The C struct of schedule s (default: the calling thread's current schedule)."""
+    s = get_schedule() if s is None else s
+    return native.RenderSchedule(s.fwd_batch, s.fwd_warps, s.bwd_batch, 0)
+
+
 def set_schedule(s: Schedule) -> None:
+    """Makes s the schedule of the calling thread's later rasteriser calls (checked by the
+    library: an unsupported shape raises)."""
     lib = native.load()
-    native.check(lib.cfgs_set_render_schedule(native.C.byref(native.RenderSchedule(s.fwd_batch, s.fwd_warps,
-                                                                                    s.bwd_batch, 0))),
-                 "cfgs_set_render_schedule")
+    native.check(lib.cfgs_render_schedule_check(native.C.byref(c_schedule(s)), None), "cfgs_render_schedule_check")
+    _thread.schedule = s
 
 
 def get_schedule() -> Schedule:
-    lib = native.load()
-    r = native.RenderSchedule()
-    lib.cfgs_get_render_schedule(native.C.byref(r))
-    return Schedule(int(r.fwd_batch), int(r.fwd_warps), int(r.bwd_batch))
+    """The calling thread's current schedule (DEFAULT until set)."""
+    return getattr(_thread, "schedule", DEFAULT)
 
 
 @contextmanager
 def using(s: Schedule):
-    """Runs the body under schedule s and restores the previous one."""
+    """Runs the body under schedule s (in this thread) and restores the previous one."""
     old = get_schedule()
     set_schedule(s)
     try:
@@ -212,7 +226,8 @@ def tune_rasterizer(raster_settings, means3D, opacities, shs=None, colors_precom
                     rotations=None, cov3D_precomp=None, tuner: Autotuner | None = None,
                     apply: bool = True) -> Schedule:
     """Tunes the render schedule for one drop-in rasteriser workload (forward + backward
-    with a unit image gradient) and, with apply=True, makes it the process-wide schedule."""
+    with a unit image gradient) and, with apply=True, makes it the calling thread's
+    schedule."""
     import torch
     from . import raster
     tuner = tuner or Autotuner()

@@ -36,6 +36,13 @@ class BatchResult:
     retries: int
 
 
+def _raise_on_timeout(flags: int) -> None:
+    """A kernel's bounded wait for an on-chip copy ran out: the iterations' results are
+    invalid."""
+    if flags & native.FLAG_COPY_TIMEOUT:
+        raise RuntimeError(f"a bounded device wait ran out (flags 0x{flags:x}); the batch's results are invalid")
+
+
 class BatchSolver:
     """Packs `problems` (device-resident PoseProblem objects with equal SH width) into
     one batch. Call solve(iters) to run them."""
@@ -154,6 +161,8 @@ class BatchSolver:
         a.pose_partials, a.xi, a.adam_state = self.partials.data_ptr(), self.xi.data_ptr(), self.adam.data_ptr()
         a.pose_states = self.pose_states.data_ptr()
         a.lr, a.beta1, a.beta2, a.eps = self.lr, float(self.betas[0]), float(self.betas[1]), self.eps
+        # this batch's tuned schedule, else the calling thread's current one
+        a.schedule = autotune_mod.c_schedule(self.schedule)
         return a
 
     def _counts(self) -> native.Counts:
@@ -171,9 +180,10 @@ class BatchSolver:
         self.xi.copy_(xi)
         self.adam.copy_(adam)
 
-    def _apply_schedule(self, args) -> None:
-        """Sets the render schedule for this batch's shape (tuning it on the batch when
-        the cache has none); the solves' state is left as it was."""
+    def _apply_schedule(self) -> None:
+        """Sets this batch's render schedule for its shape (tuning it on the batch when
+        the cache has none); the solves' state is left as it was. Without a tuner the
+        batch uses the calling thread's current schedule."""
         if self.tuner is None:
             return
         key = autotune_mod.batch_key(int(sum(int(p.xyz.shape[0]) for p in self.problems)), int(self.plan.num_tiles),
@@ -182,8 +192,11 @@ class BatchSolver:
         if sched is None:
             saved = (self.xi.clone(), self.adam.clone())
             dev = self.dev
+            self.schedule = None
+            args = self._args()
 
-            def run():
+            def run():  # one iteration under the schedule the tuner is timing (this thread's)
+                args.schedule = autotune_mod.c_schedule()
                 native.check(self.lib.cfgs_batch_iteration(C.byref(args), torch.cuda.current_stream(dev).cuda_stream),
                              "cfgs_batch_iteration")
 
@@ -191,7 +204,6 @@ class BatchSolver:
                          "cfgs_batch_init")
             sched = self.tuner.tune(key, run)
             self.load_state(*saved)
-        autotune_mod.set_schedule(sched)
         self.schedule = sched
 
     def launch(self, iters: int) -> torch.cuda.Event:
@@ -204,9 +216,9 @@ class BatchSolver:
             self.load_state(self._saved[0], self._saved[1])
             self._alloc_instances(int(K0 * self.capacity_factor) + 4096)
             self._cap_ready = True
+        self._apply_schedule()
         args = self._args()
         st = torch.cuda.current_stream(self.dev).cuda_stream
-        self._apply_schedule(args)
         native.check(self.lib.cfgs_batch_init(C.byref(args), st), "cfgs_batch_init")
         done = self._run_graph(args, iters) if (self.use_graph and iters >= self.graph_chunk) else 0
         for _ in range(iters - done):
@@ -218,7 +230,9 @@ class BatchSolver:
     def finish(self) -> bool:
         """After launch()'s event: True if the iterations ran within capacity; otherwise
         restores the state saved by launch() and doubles the capacity (re-launch)."""
-        if not (self._counts().flags & native.FLAG_CAPACITY_OVERFLOW):
+        flags = self._counts().flags
+        _raise_on_timeout(flags)
+        if not (flags & native.FLAG_CAPACITY_OVERFLOW):
             return True
         self.load_state(self._saved[0], self._saved[1])
         self._alloc_instances(self.capacity * 2)
@@ -268,9 +282,9 @@ class BatchSolver:
         while True:
             self.reset()
             self._alloc_instances(cap)
+            self._apply_schedule()
             args = self._args()
             st = torch.cuda.current_stream(self.dev).cuda_stream
-            self._apply_schedule(args)
             native.check(self.lib.cfgs_batch_init(C.byref(args), st), "cfgs_batch_init")
             t0 = time.perf_counter()
             if self.use_graph and iters >= self.graph_chunk:
@@ -283,6 +297,7 @@ class BatchSolver:
             torch.cuda.synchronize(self.dev)
             dt = time.perf_counter() - t0
             c = self._counts()
+            _raise_on_timeout(c.flags)
             if c.flags & native.FLAG_CAPACITY_OVERFLOW and retries < 3:
                 retries += 1
                 cap *= 2

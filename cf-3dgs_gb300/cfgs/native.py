@@ -21,9 +21,14 @@ STATUS = {
 }
 FLAG_FRUSTUM_VIOLATION = 0x1
 FLAG_CAPACITY_OVERFLOW = 0x2
+FLAG_COPY_TIMEOUT = 0x4
 
 _vp = C.c_void_p
 _fp = C.c_void_p  # device float* passed as an address
+
+
+class RenderSchedule(C.Structure):
+    _fields_ = [("fwd_batch", C.c_int32), ("fwd_warps", C.c_int32), ("bwd_batch", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Settings(C.Structure):
@@ -40,6 +45,7 @@ class Settings(C.Structure):
         ("campos", _fp),
         ("prefiltered", C.c_int32),
         ("debug", C.c_int32),
+        ("schedule", RenderSchedule),
     ]
 
 
@@ -74,10 +80,6 @@ class Counts(C.Structure):
     _fields_ = [("num_rendered", C.c_uint32), ("flags", C.c_uint32)]
 
 
-class RenderSchedule(C.Structure):
-    _fields_ = [("fwd_batch", C.c_int32), ("fwd_warps", C.c_int32), ("bwd_batch", C.c_int32), ("reserved", C.c_int32)]
-
-
 class BatchScene(C.Structure):
     _fields_ = [("image_width", C.c_int32), ("image_height", C.c_int32), ("tanfovx", C.c_float),
                 ("tanfovy", C.c_float), ("viewmatrix", _fp), ("projmatrix", _fp), ("campos", _fp), ("bg", _fp),
@@ -98,7 +100,7 @@ class BatchArgs(C.Structure):
                 ("rotations", _vp), ("target", _vp), ("color", _vp), ("radii", _vp), ("geom", _vp), ("image", _vp),
                 ("binning", _vp), ("scratch", _vp), ("pose_partials", _vp), ("xi", _vp), ("adam_state", _vp),
                 ("pose_states", _vp), ("lr", C.c_double), ("beta1", C.c_double), ("beta2", C.c_double),
-                ("eps", C.c_double)]
+                ("eps", C.c_double), ("schedule", RenderSchedule)]
 
 
 EXPORTS = {
@@ -147,8 +149,8 @@ EXPORTS = {
     "cfgs_ssim_scratch_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     "cfgs_ssim_forward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_ssim_backward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
-    "cfgs_set_render_schedule": (C.c_int, [C.POINTER(RenderSchedule)]),
-    "cfgs_get_render_schedule": (None, [C.POINTER(RenderSchedule)]),
+    "cfgs_render_schedule_check": (C.c_int, [C.POINTER(RenderSchedule), C.POINTER(RenderSchedule)]),
+    "cfgs_diag_copy_timeout": (C.c_int, [C.c_uint32, _vp, _vp]),
     "cfgs_l1_loss_scratch_bytes": (C.c_size_t, [C.c_int64]),
     "cfgs_l1_loss_forward": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, _vp, _vp]),
     "cfgs_l1_loss_backward": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, _vp]),

@@ -10,7 +10,7 @@ from dataclasses import dataclass
 
 import torch
 
-from . import native
+from . import autotune, native
 
 _EMPTY = None
 
@@ -39,9 +39,10 @@ def stream_handle(device: torch.device) -> int:
     return torch.cuda.current_stream(device).cuda_stream
 
 
-def make_settings(rs, keep: list) -> native.Settings:
+def make_settings(rs, keep: list, schedule=None) -> native.Settings:
     """Packs a GaussianRasterizationSettings into the C struct. Tensors are made
-    contiguous float32 and appended to `keep` so they outlive the call."""
+    contiguous float32 and appended to `keep` so they outlive the call. The render
+    schedule is `schedule` (an autotune.Schedule) or the calling thread's current one."""
     bg = _f32(rs.bg)
     view = _f32(rs.viewmatrix)
     proj = _f32(rs.projmatrix)
@@ -60,6 +61,7 @@ def make_settings(rs, keep: list) -> native.Settings:
     s.campos = _ptr(campos)
     s.prefiltered = int(bool(rs.prefiltered))
     s.debug = int(bool(rs.debug))
+    s.schedule = autotune.c_schedule() if schedule is None else autotune.c_schedule(schedule)
     return s
 
 
@@ -298,7 +300,8 @@ def kernel_launches(width: int, height: int) -> dict:
     """Kernels the forward and backward launch for one image (N > 0): preprocess and
     the K sum; binning = depth sort (4 radix passes of count/scan/scatter), rank sums,
     emission, tile sort (count/scan/scatter per pass of at most 8 tile-index bits) and
-    tile ranges; compositing; render backward; preprocess backward."""
+    tile ranges; compositing; render backward; preprocess backward. (Memory clears the
+    library enqueues with cudaMemsetAsync are not counted.)"""
     tiles = ((width + 15) // 16) * ((height + 15) // 16)
     bits = 1
     while bits < 31 and (1 << bits) < tiles:

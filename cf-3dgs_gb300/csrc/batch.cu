@@ -125,6 +125,8 @@ extern "C" int cfgs_batch_init(const CfgsBatchArgs* a, void* stream) {
 
 extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   if (!args_ok(a)) return CFGS_ERR_INVALID_ARGUMENT;
+  CfgsRenderSchedule sched;
+  if (!resolve_schedule(a->schedule, &sched)) return CFGS_ERR_INVALID_ARGUMENT;
   cudaStream_t st = (cudaStream_t)stream;
   BatchViews v = views(a);
   if (cudaMemsetAsync(v.iv.counts, 0, sizeof(CfgsCounts), st) != cudaSuccess) return CFGS_ERR_LAUNCH;
@@ -176,6 +178,7 @@ extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   ra.out_alpha = nullptr;
   ra.cap = a->capacity;
   ra.counts = v.iv.counts;
+  ra.sched = sched;
   launch_render_fwd(ra, a->num_tiles, st);
 
   RenderBwdArgs<SceneTable> rb;
@@ -193,9 +196,13 @@ extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   rb.dL_dalpha = nullptr;
   rb.color = a->color;
   rb.target = a->target;
-  rb.records = static_cast<float4*>(a->scratch);
+  const ScratchLayout SL(a->capacity);
+  rb.records = reinterpret_cast<float4*>(static_cast<char*>(a->scratch) + SL.records);
+  rb.written = reinterpret_cast<uint8_t*>(static_cast<char*>(a->scratch) + SL.written);
+  if (a->capacity > 0 && cudaMemsetAsync(rb.written, 0, (size_t)a->capacity, st) != cudaSuccess) return CFGS_ERR_LAUNCH;
   rb.cap = a->capacity;
   rb.counts = v.iv.counts;
+  rb.sched = sched;
   launch_render_bwd(rb, a->num_tiles, st);
 
   PreBwdArgs<SceneTable> pb;
@@ -203,7 +210,8 @@ extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   pb.g = g;
   pb.radii = a->radii;
   pb.geom = v.gv;
-  pb.records = static_cast<const float4*>(a->scratch);
+  pb.records = rb.records;
+  pb.written = rb.written;
   pb.out = CfgsGradients{};
   pb.total_slots = a->gauss_slots;
   pb.cap = a->capacity;

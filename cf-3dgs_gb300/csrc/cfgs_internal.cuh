@@ -297,7 +297,21 @@ inline SceneDesc single_scene_desc(const CfgsSettings* s, int32_t n, int32_t sh_
 
 // Backward scratch: one 48-byte record per pre-sort instance:
 // (dxy.x, dxy.y, dconic.a, dconic.b) (dconic.c, dopacity, drgb.r, drgb.g) (drgb.b, ddepth, 0, 0)
+// and one byte per instance that says whether the record was written. The render
+// backward writes the records of the instances some warp of their tile kept (the others'
+// gradients are exact zeros) and sets their bytes; the bytes start at zero (cleared
+// before the render backward), so the preprocess backward reads only written records.
 constexpr int kRecordFloat4 = 3;
+
+struct ScratchLayout {
+  size_t records, written, total;
+  __host__ __device__ explicit ScratchLayout(int64_t cap) {
+    const size_t c = (size_t)(cap > 0 ? cap : 1);
+    records = 0;
+    written = align256(sizeof(float) * 4 * kRecordFloat4 * c);
+    total = align256(written + c);
+  }
+};
 
 // ---------------------------------------------------------------------------
 // Scalar math whose exact rounding sequence the CPU oracle reproduces.
@@ -459,9 +473,11 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Bounded wait for phase `parity` of an mbarrier; false if it did not complete.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 22); ++it) {
+// Bounded wait for phase `parity` of an mbarrier: at most max_polls try_wait polls; false
+// if the phase did not complete (the caller raises an error flag and carries on).
+constexpr uint32_t kMbarMaxPolls = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t max_polls = kMbarMaxPolls) {
+  for (uint32_t it = 0; it < max_polls; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"

@@ -58,6 +58,7 @@ struct RenderArgs {
   float* out_alpha;
   int64_t cap;
   const CfgsCounts* counts;
+  CfgsRenderSchedule sched;  // resolved launch shape (resolve_schedule)
 };
 
 // Render backward. The per-pixel image gradient comes either from dL_dcolor (layout
@@ -81,8 +82,10 @@ struct RenderBwdArgs {
   const float* color;   // forward output (fused L1 only)
   const float* target;  // fused L1 target, or NULL
   float4* records;
+  uint8_t* written;     // per instance: 1 when its record was written (zeroed beforehand)
   int64_t cap;
   const CfgsCounts* counts;
+  CfgsRenderSchedule sched;  // resolved launch shape (resolve_schedule)
 };
 
 template <class Scenes>
@@ -92,6 +95,7 @@ struct PreBwdArgs {
   const int32_t* radii;
   GeomView geom;
   const float4* records;
+  const uint8_t* written;  // records whose byte is 0 are exact zeros and are not read
   CfgsGradients out;
   int64_t total_slots;
   int64_t cap;
@@ -114,8 +118,9 @@ template <class Scenes>
 void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st);
 template <class Scenes>
 void launch_preprocess_bwd(const PreBwdArgs<Scenes>& a, int blocks, cudaStream_t st);
-// The process-wide render schedule (cfgs_set_render_schedule), read at launch time.
-CfgsRenderSchedule render_schedule();
+// The schedule a call uses: zeros become the default {128, 4, 64}; false when the
+// combination is not one the render kernels are instantiated for.
+bool resolve_schedule(const CfgsRenderSchedule& in, CfgsRenderSchedule* out);
 
 void launch_batch_pose_init(int count, const float* xi, const float* adam_state, PoseState* states, double b1,
                             double b2, cudaStream_t st);

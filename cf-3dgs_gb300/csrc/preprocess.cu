@@ -344,7 +344,7 @@ extern "C" size_t cfgs_image_bytes(int32_t w, int32_t h) {
 }
 extern "C" size_t cfgs_binning_bytes(int64_t cap) { return cap < 0 ? 0 : BinningLayout(cap).total; }
 extern "C" size_t cfgs_backward_scratch_bytes(int64_t cap) {
-  return align256(sizeof(float) * 4 * kRecordFloat4 * (size_t)(cap > 0 ? cap : 1));
+  return ScratchLayout(cap).total;
 }
 
 extern "C" void cfgs_geom_layout(int32_t n, size_t o[14]) {
@@ -397,7 +397,7 @@ extern "C" int cfgs_preprocess_forward(const CfgsSettings* s, const CfgsGaussian
     k_preprocess<SingleScene><<<GL.num_blocks, kPreprocessBlock, 0, st>>>(a);
     CFGS_CHECK_LAUNCH(s->debug, st);
   }
-  k_scan<<<1, 1024, 0, st>>>(gv.block_sums, GL.num_blocks, iv.counts);
+  launch_scan(gv.block_sums, GL.num_blocks, iv.counts, st);
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;
 }

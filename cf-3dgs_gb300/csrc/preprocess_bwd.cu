@@ -5,8 +5,9 @@
 //
 // Phase 1 sums each Gaussian's per-tile records (contiguous: instance indices
 // [offset, offset + touched)) eight lanes per Gaussian, four Gaussians per warp at a
-// time: strided 48-byte record loads, a transposing reduction inside each group of
-// eight lanes, the sums to shared memory. Phase 2 is one thread per Gaussian. Both
+// time: strided 48-byte record loads of the records the render backward wrote (one byte
+// per instance says which), a transposing reduction inside each group of eight lanes,
+// the sums to shared memory. Phase 2 is one thread per Gaussian. Both
 // orders are fixed, so the result is deterministic.
 #include "cfgs_internal.cuh"
 #include "kernels.cuh"
@@ -232,12 +233,15 @@ __device__ __forceinline__ void gaussian_backward(const PreBwdArgs<Scenes>& a, c
     const float cc = T1[0] * v[0] + T1[1] * v[1] + T1[2] * v[2] + 0.3f;
 
     // ---- conic (A,B,C) -> 2D covariance (a,b,c) -----------------------------------
+    // With A = c/det, B = -b/det, C = a/det: dC/da = dA/dc = 1/det - ac/det^2, which is
+    // -b^2/det^2 exactly; written that way it carries no cancellation (near-isotropic
+    // conics, b ~ 0, would otherwise lose the term to the rounding of 1/det).
     const float dA = acc[2], dB = acc[3], dC = acc[4];
     const float det = ca * cc - cb * cb;
     const float id = 1.f / det, id2 = id * id;
-    const float da = dA * (-cc * cc * id2) + dB * (cb * cc * id2) + dC * (id - ca * cc * id2);
+    const float da = dA * (-cc * cc * id2) + dB * (cb * cc * id2) + dC * (-(cb * cb) * id2);
     const float db = dA * (2.f * cb * cc * id2) + dB * (-id - 2.f * cb * cb * id2) + dC * (2.f * ca * cb * id2);
-    const float dc = dA * (id - ca * cc * id2) + dB * (ca * cb * id2) + dC * (-ca * ca * id2);
+    const float dc = dA * (-(cb * cb) * id2) + dB * (ca * cb * id2) + dC * (-ca * ca * id2);
 
     // ---- 2D covariance -> 3D covariance and the rows of T = J W ------------------
     float dcov[6];
@@ -416,6 +420,7 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
 #pragma unroll
       for (int k = 0; k < 16; ++k) v[k] = 0.f;
       for (uint32_t r = sub; r < nt; r += 8) {
+        if (!a.written[off + r]) continue;  // exact-zero record, never written
         const float4* rec = a.records + (size_t)kRecordFloat4 * (off + r);
         const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
         v[0] += r0.x; v[1] += r0.y; v[2] += r0.z; v[3] += r0.w;
@@ -515,3 +520,35 @@ template void launch_preprocess_bwd<SingleScene>(const PreBwdArgs<SingleScene>&,
 template void launch_preprocess_bwd<SceneTable>(const PreBwdArgs<SceneTable>&, int, cudaStream_t);
 
 }  // namespace cfgs
+
+// ---- diagnostics: the bounded copy wait --------------------------------------------
+namespace cfgs {
+
+// One thread arms an mbarrier for `bytes` of transfer that no copy ever delivers and
+// waits on it with the library's bounded wait (max_polls polls), exactly as the kernels
+// wait for their bulk and tensor copies; when the wait gives up it raises
+// CFGS_FLAG_COPY_TIMEOUT in *flags. No copy is issued, so nothing is in flight when the
+// block exits.
+__global__ void __launch_bounds__(32) k_copy_wait_diag(uint32_t max_polls, uint32_t bytes, uint32_t* flags) {
+  __shared__ __align__(8) uint64_t s_bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t bar = smem_addr(&s_bar);
+  mbar_init(bar, 1);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+  if (!mbar_wait(bar, 0, max_polls)) atomicOr(flags, CFGS_FLAG_COPY_TIMEOUT);
+}
+
+}  // namespace cfgs
+
+extern "C" int cfgs_diag_copy_timeout(uint32_t max_polls, uint32_t* flags, void* stream) {
+  if (!flags || max_polls == 0 || max_polls > cfgs::kMbarMaxPolls) return CFGS_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemsetAsync(flags, 0, sizeof(uint32_t), st) != cudaSuccess) return CFGS_ERR_LAUNCH;
+  cfgs::k_copy_wait_diag<<<1, 32, 0, st>>>(max_polls, 1024u, flags);
+  if (cudaGetLastError() != cudaSuccess) return CFGS_ERR_LAUNCH;
+  uint32_t host = 0;
+  if (cudaMemcpyAsync(&host, flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return CFGS_ERR_LAUNCH;
+  return (host & CFGS_FLAG_COPY_TIMEOUT) ? CFGS_ERR_DEVICE_FLAG : CFGS_OK;
+}

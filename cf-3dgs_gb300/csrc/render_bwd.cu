@@ -332,20 +332,23 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
       float sum[10];
 #pragma unroll
       for (int q = 0; q < 10; ++q) sum[q] = 0.f;
+      bool kept = false;
 #pragma unroll
       for (int w = 0; w < kWarps; ++w)
-        if ((s_keep[w][j >> 5] >> (j & 31)) & 1u)
+        if ((s_keep[w][j >> 5] >> (j & 31)) & 1u) {
+          kept = true;
 #pragma unroll
           for (int q = 0; q < 10; ++q) sum[q] += s_part[w][j][q];
-      finish_record(a.records + (size_t)kRecordFloat4 * s_pidx[cur][j], sum, s_co_b[j]);
+        }
+      // An instance no warp kept has exact-zero gradients: no record, its byte stays 0.
+      if (kept) {
+        const uint32_t pidx = s_pidx[cur][j];
+        finish_record(a.records + (size_t)kRecordFloat4 * pidx, sum, s_co_b[j]);
+        a.written[pidx] = 1;
+      }
     }
   }
-  for (int i = max_last + threadIdx.x; i < n; i += blockDim.x) {
-    float4* rec = a.records + (size_t)kRecordFloat4 * a.sorted_pidx[lo + i];
-    rec[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-    rec[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-    rec[2] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
+  // Instances at or past the tile's last contributor reach no pixel: nothing to write.
 }
 
 template <class Scenes, bool DEPTH>
@@ -357,7 +360,7 @@ void launch_render_bwd_depth(const RenderBwdArgs<Scenes>& a, int tiles, int batc
 
 template <class Scenes>
 void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st) {
-  const int batch = render_schedule().bwd_batch;
+  const int batch = a.sched.bwd_batch;
   if constexpr (Scenes::kBatched) {  // batched solves never ask for depth gradients
     launch_render_bwd_depth<Scenes, false>(a, tiles, batch, st);
   } else {
@@ -399,9 +402,13 @@ extern "C" int cfgs_render_backward(const CfgsSettings* s, int32_t num_gaussians
   ra.dL_dalpha = dL_dalpha;
   ra.color = nullptr;
   ra.target = nullptr;
-  ra.records = static_cast<float4*>(scratch);
+  const ScratchLayout SL(capacity);
+  ra.records = reinterpret_cast<float4*>(static_cast<char*>(scratch) + SL.records);
+  ra.written = reinterpret_cast<uint8_t*>(static_cast<char*>(scratch) + SL.written);
   ra.cap = capacity;
   ra.counts = iv.counts;
+  if (!resolve_schedule(s->schedule, &ra.sched)) return CFGS_ERR_INVALID_ARGUMENT;
+  if (capacity > 0 && cudaMemsetAsync(ra.written, 0, (size_t)capacity, st) != cudaSuccess) return CFGS_ERR_LAUNCH;
   launch_render_bwd(ra, IL.num_tiles, st);
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;
@@ -428,7 +435,9 @@ extern "C" int cfgs_preprocess_backward(const CfgsSettings* s, const CfgsGaussia
   pa.g = *g;
   pa.radii = radii;
   pa.geom = GeomView(const_cast<void*>(geom), g->num_gaussians);
-  pa.records = static_cast<const float4*>(scratch);
+  const ScratchLayout SL(capacity);
+  pa.records = reinterpret_cast<const float4*>(static_cast<const char*>(scratch) + SL.records);
+  pa.written = reinterpret_cast<const uint8_t*>(static_cast<const char*>(scratch) + SL.written);
   pa.out = *out;
   pa.total_slots = g->num_gaussians;
   pa.cap = capacity;
@@ -458,29 +467,74 @@ extern "C" int cfgs_backward(const CfgsSettings* s, const CfgsGaussians* g, cons
 // Some callers cannot allocate device memory when they call the rasteriser: plugin
 // hosts that hand a plugin only its input and output buffers, and services that must
 // not allocate once they are serving. This entry point runs the same two kernels as
-// cfgs_backward, but the per-instance gradient records live in the fixed array below
-// instead of a caller-provided scratch buffer. Every GPU that loads this library holds
-// the array (30 MiB) until the process exits.
-static __device__ __align__(256) float4 g_noalloc_records[(size_t)CFGS_NOALLOC_MAX_INSTANCES * kRecordFloat4];
+// cfgs_backward, but its per-instance scratch (gradient records and their written
+// bytes, the layout cfgs_backward_scratch_bytes sizes) lives in the fixed array below
+// instead of a caller-provided buffer. Every GPU that loads this library holds the
+// array (30.6 MiB) until the process exits.
+constexpr size_t kNoallocRecordBytes = ((size_t)CFGS_NOALLOC_MAX_INSTANCES * 16 * kRecordFloat4 + 255) & ~size_t(255);
+constexpr size_t kNoallocScratchBytes = kNoallocRecordBytes + (((size_t)CFGS_NOALLOC_MAX_INSTANCES + 255) & ~size_t(255));
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
 namespace {
-constexpr int kNoallocMaxDevices = 64;
+// The array's device address belongs to the CUDA context that loaded this library's
+// device code: after cudaDeviceReset, or in another context on the same device, the
+// module is loaded again and the array may sit elsewhere. So the address is cached per
+// context, keyed by the driver's context id (unique for the life of the process, even
+// when a new context reuses a freed one's handle), and looked up again for a context
+// not seen before. The driver functions come through the runtime's entry-point query,
+// so the library does not link the driver library itself.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+constexpr int kNoallocCacheSize = 64;
+struct NoallocEntry {
+  unsigned long long ctx_id;
+  void* ptr;
+};
 std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kNoallocMaxDevices] = {};
+NoallocEntry g_noalloc_cache[kNoallocCacheSize];
+int g_noalloc_used = 0, g_noalloc_next = 0;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
 
-// Device address of g_noalloc_records on the current device. The host-side name of
-// the array is only a stand-in, so the address is looked up once per device, with
-// that device current, and cached.
-int noalloc_records(void** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices) return CFGS_ERR_LAUNCH;
+bool context_id(unsigned long long* id) {
+  void* ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != 0 || ctx == nullptr) return false;
+  return g_ctx_get_id(ctx, id) == 0;
+}
+
+// Device address of g_noalloc_scratch in the current context. The host-side name of
+// the array is only a stand-in for it, so the address comes from cudaGetSymbolAddress,
+// called with the caller's device current, once per context.
+int noalloc_scratch(void** out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_ptr[dev] == nullptr) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_records) != cudaSuccess || p == nullptr) return CFGS_ERR_LAUNCH;
-    g_noalloc_ptr[dev] = p;
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", reinterpret_cast<void**>(&g_ctx_get_current), 12000,
+                                         cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", reinterpret_cast<void**>(&g_ctx_get_id), 12000,
+                                         cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess) {
+      g_ctx_get_current = nullptr;
+      g_ctx_get_id = nullptr;
+      return CFGS_ERR_LAUNCH;
+    }
   }
-  *out = g_noalloc_ptr[dev];
+  unsigned long long id = 0;
+  const bool have_ctx = context_id(&id);
+  if (have_ctx)
+    for (int i = 0; i < g_noalloc_used; ++i)
+      if (g_noalloc_cache[i].ctx_id == id) {
+        *out = g_noalloc_cache[i].ptr;
+        return CFGS_OK;
+      }
+  // Not seen yet (or no context current: the lookup below makes the device's primary
+  // context current and loads the module).
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return CFGS_ERR_LAUNCH;
+  if (!context_id(&id)) return CFGS_ERR_LAUNCH;
+  const int slot = g_noalloc_used < kNoallocCacheSize ? g_noalloc_used++ : (g_noalloc_next++ % kNoallocCacheSize);
+  g_noalloc_cache[slot] = NoallocEntry{id, p};
+  *out = p;
   return CFGS_OK;
 }
 }  // namespace
@@ -491,9 +545,9 @@ extern "C" int cfgs_backward_noalloc(const CfgsSettings* s, const CfgsGaussians*
                                      const CfgsGradients* out, void* stream) {
   if (capacity < 0) return CFGS_ERR_INVALID_ARGUMENT;
   if (capacity > CFGS_NOALLOC_MAX_INSTANCES) return CFGS_ERR_TOO_LARGE;
-  void* records = nullptr;
-  int st = noalloc_records(&records);
+  void* scratch = nullptr;
+  int st = noalloc_scratch(&scratch);
   if (st != CFGS_OK) return st;
-  return cfgs_backward(s, g, radii, geom, image, binning, capacity, records, dL_dcolor, dL_ddepth, dL_dalpha, out,
+  return cfgs_backward(s, g, radii, geom, image, binning, capacity, scratch, dL_dcolor, dL_ddepth, dL_dalpha, out,
                        stream);
 }

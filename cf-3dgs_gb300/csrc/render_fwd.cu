@@ -5,8 +5,6 @@
 // descriptor table for batched solves); the arithmetic is the same for both.
 // Compiled with -fmad=false; the fmaf() calls are the only fused operations, and the
 // CPU oracle performs the same sequence.
-#include <mutex>
-
 #include "cfgs_internal.cuh"
 #include "kernels.cuh"
 
@@ -168,7 +166,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_render_fwd(RenderArgs<Scenes> a)
 
 template <class Scenes>
 void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st) {
-  const CfgsRenderSchedule rs = render_schedule();
+  const CfgsRenderSchedule& rs = a.sched;
   if (rs.fwd_warps == 8) {
     if (rs.fwd_batch == 256) k_render_fwd<Scenes, 256, 8><<<tiles, 256, 0, st>>>(a);
     else k_render_fwd<Scenes, 128, 8><<<tiles, 256, 0, st>>>(a);
@@ -181,37 +179,29 @@ void launch_render_fwd(const RenderArgs<Scenes>& a, int tiles, cudaStream_t st) 
 template void launch_render_fwd<SingleScene>(const RenderArgs<SingleScene>&, int, cudaStream_t);
 template void launch_render_fwd<SceneTable>(const RenderArgs<SceneTable>&, int, cudaStream_t);
 
-}  // namespace cfgs
-
-namespace cfgs {
-
-namespace {
-std::mutex g_schedule_mu;
-CfgsRenderSchedule g_schedule{kRenderBatch, 4, 64, 0};
-}  // namespace
-
-CfgsRenderSchedule render_schedule() {
-  std::lock_guard<std::mutex> lk(g_schedule_mu);
-  return g_schedule;
+bool resolve_schedule(const CfgsRenderSchedule& in, CfgsRenderSchedule* out) {
+  if (in.fwd_batch == 0 && in.fwd_warps == 0 && in.bwd_batch == 0) {
+    *out = CfgsRenderSchedule{kRenderBatch, 4, 64, 0};
+    return true;
+  }
+  const bool fwd_ok = in.fwd_warps == 4 ? (in.fwd_batch == 64 || in.fwd_batch == 128 || in.fwd_batch == 256)
+                                        : (in.fwd_warps == 8 && (in.fwd_batch == 128 || in.fwd_batch == 256));
+  const bool bwd_ok = in.bwd_batch == 32 || in.bwd_batch == 64 || in.bwd_batch == 128;
+  if (!fwd_ok || !bwd_ok) return false;
+  *out = CfgsRenderSchedule{in.fwd_batch, in.fwd_warps, in.bwd_batch, 0};
+  return true;
 }
 
 }  // namespace cfgs
 
 using namespace cfgs;
 
-extern "C" int cfgs_set_render_schedule(const CfgsRenderSchedule* s) {
+extern "C" int cfgs_render_schedule_check(const CfgsRenderSchedule* s, CfgsRenderSchedule* resolved) {
   if (!s) return CFGS_ERR_INVALID_ARGUMENT;
-  const bool fwd_ok = s->fwd_warps == 4 ? (s->fwd_batch == 64 || s->fwd_batch == 128 || s->fwd_batch == 256)
-                                        : (s->fwd_warps == 8 && (s->fwd_batch == 128 || s->fwd_batch == 256));
-  const bool bwd_ok = s->bwd_batch == 32 || s->bwd_batch == 64 || s->bwd_batch == 128;
-  if (!fwd_ok || !bwd_ok) return CFGS_ERR_INVALID_ARGUMENT;
-  std::lock_guard<std::mutex> lk(g_schedule_mu);
-  g_schedule = CfgsRenderSchedule{s->fwd_batch, s->fwd_warps, s->bwd_batch, 0};
+  CfgsRenderSchedule r;
+  if (!resolve_schedule(*s, &r)) return CFGS_ERR_INVALID_ARGUMENT;
+  if (resolved) *resolved = r;
   return CFGS_OK;
-}
-
-extern "C" void cfgs_get_render_schedule(CfgsRenderSchedule* s) {
-  if (s) *s = render_schedule();
 }
 
 extern "C" int cfgs_composite_forward(const CfgsSettings* s, int32_t num_gaussians, const void* geom, const void* image,
@@ -240,6 +230,7 @@ extern "C" int cfgs_composite_forward(const CfgsSettings* s, int32_t num_gaussia
   ra.out_alpha = out_alpha;
   ra.cap = capacity;
   ra.counts = iv.counts;
+  if (!resolve_schedule(s->schedule, &ra.sched)) return CFGS_ERR_INVALID_ARGUMENT;
   launch_render_fwd(ra, IL.num_tiles, st);
   CFGS_CHECK_LAUNCH(s->debug, st);
   return CFGS_OK;

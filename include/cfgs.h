@@ -53,8 +53,29 @@ typedef enum CfgsStatus {
 #define CFGS_TILE_X 16
 #define CFGS_TILE_Y 16
 
+/* ---- render schedule -----------------------------------------------------------------
+ * Launch shape of the two per-tile render kernels, chosen per call (a field of
+ * CfgsSettings and of CfgsBatchArgs; the library keeps no schedule of its own). Every
+ * schedule gives bit-identical results (each pixel sees the same instances in the same
+ * order with the same arithmetic, and each instance's gradient record is summed the same
+ * way), so the choice is a pure performance one; cfgs/autotune.py picks it by timing.
+ *   fwd_batch: instances staged per round in the forward: 64, 128 or 256
+ *   fwd_warps: warps per tile in the forward: 4 (8x8 pixel boxes, two pixels per
+ *              lane) or 8 (8x4 boxes, one pixel per lane; fwd_batch 128 or 256)
+ *   bwd_batch: instances staged per round in the backward: 32, 64 or 128
+ * All-zero fields mean the default {128, 4, 64}; an unsupported combination makes the
+ * call return CFGS_ERR_INVALID_ARGUMENT. */
+typedef struct CfgsRenderSchedule {
+  int32_t fwd_batch, fwd_warps, bwd_batch, reserved;
+} CfgsRenderSchedule;
+
+/* CFGS_OK when `schedule` is supported (zeros: the default), else
+ * CFGS_ERR_INVALID_ARGUMENT; `resolved` (may be NULL) receives the schedule a call uses. */
+int cfgs_render_schedule_check(const CfgsRenderSchedule* schedule, CfgsRenderSchedule* resolved);
+
 /* GaussianRasterizationSettings (NamedTuple, 12 fields, order of
- * scene/gaussian_model_cf.py:811-824). Tensor fields are device pointers. */
+ * scene/gaussian_model_cf.py:811-824) plus the render schedule of the call. Tensor
+ * fields are device pointers. */
 typedef struct CfgsSettings {
   int32_t image_height;
   int32_t image_width;
@@ -68,6 +89,7 @@ typedef struct CfgsSettings {
   const float* campos;      /* [3]  camera centre                                   */
   int32_t prefiltered;
   int32_t debug;            /* 1: synchronise and check after every kernel         */
+  CfgsRenderSchedule schedule; /* launch shape of this call's render kernels (zeros: default) */
 } CfgsSettings;
 
 /* The per-Gaussian inputs of GaussianRasterizer.forward. Exactly one of
@@ -113,7 +135,9 @@ size_t cfgs_geom_bytes(int32_t num_gaussians);
 size_t cfgs_image_bytes(int32_t image_width, int32_t image_height);
 /* Per-instance workspace ("binningBuffer" upstream) for up to `capacity` instances. */
 size_t cfgs_binning_bytes(int64_t capacity);
-/* Scratch used by cfgs_backward for up to `capacity` instances. */
+/* Scratch used by cfgs_backward for up to `capacity` instances: one 48-byte gradient
+ * record per instance and one byte per instance that marks the records written (the
+ * render backward writes only instances that reach a pixel; the others are zeros). */
 size_t cfgs_backward_scratch_bytes(int64_t capacity);
 
 /* Byte offsets of the arrays inside the workspaces, for inspection (tests, debugging;
@@ -188,8 +212,10 @@ int cfgs_backward(const CfgsSettings* settings, const CfgsGaussians* gaussians,
                   const CfgsGradients* grads, void* stream);
 
 /* The two halves of cfgs_backward: the per-tile render backward (renderCUDA backward
- * upstream) writing one record per instance into `scratch`, then the per-Gaussian
- * preprocess backward (computeCov2DCUDA + preprocessCUDA backward upstream). */
+ * upstream) writing into `scratch` one record per instance that reaches a pixel and
+ * marking it written (the marks are cleared first), then the per-Gaussian preprocess
+ * backward (computeCov2DCUDA + preprocessCUDA backward upstream) summing the marked
+ * records. */
 int cfgs_render_backward(const CfgsSettings* settings, int32_t num_gaussians, const void* geom,
                          const void* image, const void* binning, int64_t capacity, void* scratch,
                          const float* dL_dcolor, const float* dL_ddepth, const float* dL_dalpha, void* stream);
@@ -207,18 +233,31 @@ int cfgs_preprocess_backward(const CfgsSettings* settings, const CfgsGaussians* 
  * the caller passes no scratch buffer and nothing is allocated.
  *  - Limit: `capacity` (the binning capacity, >= K) at most
  *    CFGS_NOALLOC_MAX_INSTANCES instances; larger returns CFGS_ERR_TOO_LARGE.
- *  - Every GPU that loads the library holds the array (30 MiB) until the process exits.
- *  - The first call on a device looks up the array's device address (once per device,
- *    with that device current); make that first call before any stream capture.
- *  - All calls share the one array and it keeps the last call's contents (every record
- *    a call needs is written by that call). Calls that overlap on the GPU race with
- *    each other: serialise them, e.g. on one stream. */
+ *  - Every GPU that loads the library holds the array (30.6 MiB) until the process exits.
+ *  - The first call in a CUDA context looks up the array's device address (with the
+ *    caller's device current) and caches it for that context; a context not seen before
+ *    (a new one after cudaDeviceReset, or another context on the device) is looked up
+ *    again. Make the first call of each context before any stream capture.
+ *  - All calls share the one array and it keeps the last call's contents; each call
+ *    clears what must start at zero (the per-instance "written" bytes) and writes every
+ *    record it reads. Calls that overlap on the GPU race with each other: serialise
+ *    them, e.g. on one stream. */
 #define CFGS_NOALLOC_MAX_INSTANCES 655360
 int cfgs_backward_noalloc(const CfgsSettings* settings, const CfgsGaussians* gaussians,
                           const int32_t* radii, const void* geom, const void* image,
                           const void* binning, int64_t capacity, const float* dL_dcolor,
                           const float* dL_ddepth, const float* dL_dalpha,
                           const CfgsGradients* grads, void* stream);
+
+/* ---- diagnostics -----------------------------------------------------------------
+ * No counterpart in the reference: a check of this library's failure handling.
+ * The kernels that stage data by bulk or tensor copies wait for them on an mbarrier
+ * with a bounded number of polls; a wait that gives up raises CFGS_FLAG_COPY_TIMEOUT and
+ * the kernel returns, leaving the context usable. cfgs_diag_copy_timeout runs that same
+ * wait, with `max_polls` polls (1 .. 2^22), on an mbarrier that no copy ever completes:
+ * it writes the flags to `flags` (device uint32), synchronises `stream` and returns
+ * CFGS_ERR_DEVICE_FLAG — the expected outcome — or CFGS_OK if the wait had completed. */
+int cfgs_diag_copy_timeout(uint32_t max_polls, uint32_t* flags, void* stream);
 
 /* ---- markVisible ---------------------------------------------------------------
  * Replaces upstream mark_visible (GaussianRasterizer.markVisible): visible[i] = 1
@@ -271,23 +310,6 @@ int cfgs_ssim_forward(int32_t channels, int32_t height, int32_t width, const flo
                       void* scratch, float* ssim_mean, void* stream);
 int cfgs_ssim_backward(int32_t channels, int32_t height, int32_t width, const float* img1, const float* img2,
                        const void* scratch, const float* dL_dmean, float* dL_dimg1, void* stream);
-
-/* ---- render schedule -----------------------------------------------------------------
- * Launch shape of the two per-tile render kernels. Every schedule gives bit-identical
- * results (each pixel sees the same instances in the same order with the same
- * arithmetic, and each instance's gradient record is summed the same way), so the
- * choice is a pure performance one; cfgs/autotune.py picks it by timing.
- *   fwd_batch: instances staged per round in the forward: 64, 128 or 256
- *   fwd_warps: warps per tile in the forward: 4 (8x8 pixel boxes, two pixels per
- *              lane) or 8 (8x4 boxes, one pixel per lane; fwd_batch 128 or 256)
- *   bwd_batch: instances staged per round in the backward: 32, 64 or 128
- * Process-wide; each launch reads it when it is issued (a captured CUDA graph keeps the
- * schedule of its capture). Default {128, 4, 64}. */
-typedef struct CfgsRenderSchedule {
-  int32_t fwd_batch, fwd_warps, bwd_batch, reserved;
-} CfgsRenderSchedule;
-int cfgs_set_render_schedule(const CfgsRenderSchedule* schedule); /* INVALID_ARGUMENT if unsupported */
-void cfgs_get_render_schedule(CfgsRenderSchedule* schedule);
 
 /* ---- L1 photometric loss ------------------------------------------------------------
  * mean |x - target| over n floats (utils/loss_utils.py:15-16, trainer/losses.py:139-140),
@@ -420,6 +442,7 @@ typedef struct CfgsBatchArgs {    /* device pointers of one batch */
   float* adam_state;              /* [S][16] (cfgs_pose_adam layout)           */
   void* pose_states;              /* plan.pose_state_bytes                     */
   double lr, beta1, beta2, eps;
+  CfgsRenderSchedule schedule;    /* render kernels' launch shape (zeros: default) */
 } CfgsBatchArgs;
 
 /* Sets every solve's pose state from xi (call once before the first iteration). */

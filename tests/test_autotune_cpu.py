@@ -11,19 +11,48 @@ def test_schedule_abi_rejects_unsupported_shapes():
     from cfgs import autotune, native
     lib = native.load()
     S = native.RenderSchedule
-    old = autotune.get_schedule()
-    try:
-        for bad in [(96, 4, 64), (64, 8, 64), (128, 6, 64), (128, 4, 48), (128, 4, 256), (0, 0, 0)]:
-            assert lib.cfgs_set_render_schedule(native.C.byref(S(*bad, 0))) == 1
-        assert lib.cfgs_set_render_schedule(None) == 1
-        for good in [(64, 4, 32), (256, 8, 128), (128, 8, 64)]:
-            assert lib.cfgs_set_render_schedule(native.C.byref(S(*good, 0))) == 0
-            assert autotune.get_schedule() == autotune.Schedule(*good)
-        with autotune.using(autotune.Schedule(256, 4, 128)):
-            assert autotune.get_schedule() == autotune.Schedule(256, 4, 128)
-        assert autotune.get_schedule() == autotune.Schedule(128, 8, 64)
-    finally:
-        autotune.set_schedule(old)
+    for bad in [(96, 4, 64), (64, 8, 64), (128, 6, 64), (128, 4, 48), (128, 4, 256), (0, 4, 64)]:
+        assert lib.cfgs_render_schedule_check(native.C.byref(S(*bad, 0)), None) == 1
+    assert lib.cfgs_render_schedule_check(None, None) == 1
+    r = S()
+    assert lib.cfgs_render_schedule_check(native.C.byref(S(0, 0, 0, 0)), native.C.byref(r)) == 0
+    assert (r.fwd_batch, r.fwd_warps, r.bwd_batch) == (128, 4, 64)  # zeros: the default
+    for good in [(64, 4, 32), (256, 8, 128), (128, 8, 64)]:
+        assert lib.cfgs_render_schedule_check(native.C.byref(S(*good, 0)), native.C.byref(r)) == 0
+        assert (r.fwd_batch, r.fwd_warps, r.bwd_batch) == good
+    with pytest.raises(RuntimeError):
+        autotune.set_schedule(autotune.Schedule(96, 4, 64))
+
+
+def test_schedule_is_per_thread():
+    """The host's current schedule belongs to the calling thread; the library keeps none
+    (every call's settings carry it), so threads with different schedules do not mix."""
+    import threading
+    from cfgs import autotune, raster
+
+    class RS:  # the fields make_settings reads
+        image_height = image_width = 16
+        tanfovx = tanfovy = 1.0
+        bg = viewmatrix = projmatrix = campos = None
+        scale_modifier = 1.0
+        sh_degree = 0
+        prefiltered = debug = False
+
+    seen = {}
+
+    def worker(name, sched):
+        with autotune.using(sched):
+            s = raster.make_settings(RS, [])
+            seen[name] = (s.schedule.fwd_batch, s.schedule.fwd_warps, s.schedule.bwd_batch)
+
+    assert autotune.get_schedule() == autotune.DEFAULT
+    t1 = threading.Thread(target=worker, args=("a", autotune.Schedule(256, 8, 32)))
+    t2 = threading.Thread(target=worker, args=("b", autotune.Schedule(64, 4, 128)))
+    t1.start(), t2.start(), t1.join(), t2.join()
+    assert seen == {"a": (256, 8, 32), "b": (64, 4, 128)}
+    assert autotune.get_schedule() == autotune.DEFAULT  # this thread's is untouched
+    s = raster.make_settings(RS, [], schedule=autotune.Schedule(128, 8, 64))
+    assert (s.schedule.fwd_batch, s.schedule.fwd_warps) == (128, 8)
 
 
 def test_default_schedule_is_the_hand_tuned_one():

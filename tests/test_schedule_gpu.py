@@ -1,5 +1,5 @@
-"""Every render schedule (cfgs_set_render_schedule: forward staging batch and warps per
-tile, backward staging batch) gives bit-identical results: forward images, contributor
+"""Every render schedule (CfgsRenderSchedule, carried by each call: forward staging batch
+and warps per tile, backward staging batch) gives bit-identical results: forward images, contributor
 counts and final transmittances, every gradient of the drop-in rasteriser, and the
 poses of batched solves. The autotuner picks among them on the GPU and caches the
 choice."""
@@ -32,6 +32,7 @@ def mods():
 def _run(dgr, raster, scene, depth_grads):
     rs = settings_for(dgr, scene)
     s = scene.to(DEV)
+    torch.cuda.current_stream().synchronize()
     color, radii, depth, alpha, st = raster.forward(rs, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations,
                                                     None)
     v = raster.inspect_state(st, scene.camera.width, scene.camera.height)
@@ -91,3 +92,40 @@ def test_autotuned_batch_matches_default(mods, tmp_path):
         assert bs.schedule is not None
         assert tuner.lookup(autotune.batch_key(int(probs[0].xyz.shape[0]), bs.plan.num_tiles, bs.M)) == bs.schedule
     assert np.array_equal(got, ref)
+
+
+def test_threads_with_different_schedules_concurrently(mods):
+    """Two threads render two different workloads at the same time, each on its own
+    stream under its own schedule (the library keeps none; each call carries the
+    calling thread's): every result equals that workload's single-threaded result."""
+    import threading
+    dgr, autotune, raster, scenes = mods
+    work = {"a": (scenes.scene_small(n=16384, width=256, height=256, seed=0), autotune.Schedule(256, 8, 32)),
+            "b": (scenes.scene_small(n=2500, width=100, height=75, seed=7), autotune.Schedule(64, 4, 128))}
+    with autotune.using(autotune.DEFAULT):
+        ref = {k: _run(dgr, raster, sc, True) for k, (sc, _) in work.items()}
+    results, errors = {k: [] for k in work}, []
+    start = threading.Barrier(len(work))
+
+    def worker(name):
+        try:
+            sc, sched = work[name]
+            with torch.cuda.stream(torch.cuda.Stream()), autotune.using(sched):
+                start.wait()
+                for _ in range(4):
+                    assert autotune.get_schedule() == sched
+                    results[name].append(_run(dgr, raster, sc, True))
+        except Exception as e:  # reported below, on the main thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in work]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for name in work:
+        assert len(results[name]) == 4
+        for out in results[name]:
+            for k in ref[name]:
+                assert torch.equal(out[k], ref[name][k]), (name, k)
