@@ -20,6 +20,7 @@ structure) and renders through the drop-in forward.
 from __future__ import annotations
 
 import math
+import threading
 import time
 from collections import deque
 from dataclasses import dataclass, field
@@ -40,6 +41,8 @@ class Request:
     start: float = math.nan
     done: float = math.nan
     result: object = None
+    status: str = "pending"  # "ok", or why the request has no result: "rejected", "cancelled", "failed"
+    error: str = ""
 
     @property
     def latency(self) -> float:
@@ -122,15 +125,57 @@ class RenderTarget:
 def solve_bytes(payload: PosePayload) -> int:
     """Device memory a solve holds while active: its inputs and target, its share of the
     per-Gaussian workspace and of the per-instance workspaces (about 2 tile instances
-    per Gaussian for these scenes, 28 + 48 bytes each), and its render."""
+    per Gaussian for these scenes, 28 + 49 bytes each), and its render."""
     n = payload.xyz.shape[0]
     px = payload.target.numel() // 3
-    return payload.nbytes + n * 64 + n * 2 * 76 + px * 3 * 4 * 2 + px * 8
+    return payload.nbytes + n * 64 + n * 2 * 77 + px * 3 * 4 * 2 + px * 8
+
+
+def validate_payload(payload, hbm_budget: float = math.inf) -> str:
+    """Why a pose request cannot be served ("" when it can): shapes and dtypes of the
+    Gaussians and the target against the camera, a supported SH degree, finite values
+    (CF-3DGS stops on a NaN loss, trainer/losses.py:126-127: a request that carries one
+    is refused up front), and a device footprint within the HBM budget (a request that
+    could never be admitted is refused instead of waiting forever)."""
+    try:
+        n = int(payload.xyz.shape[0])
+        deg = int(payload.sh_degree)
+        cam = payload.camera
+        shapes = {"xyz": (payload.xyz, (n, 3)), "scales": (payload.scales, (n, 3)),
+                  "rotations": (payload.rotations, (n, 4)), "target": (payload.target, (3, cam.height, cam.width))}
+        if payload.xyz.dim() != 2 or n <= 0:
+            return "xyz must be [N,3] with N > 0"
+        if not 0 <= deg <= 3:
+            return f"SH degree {deg} is not in 0..3"
+        for name, (t, want) in shapes.items():
+            if tuple(t.shape) != want:
+                return f"{name} has shape {tuple(t.shape)}, expected {want}"
+        if tuple(payload.opacities.reshape(-1).shape) != (n,):
+            return f"opacities has {payload.opacities.numel()} values for {n} Gaussians"
+        if payload.shs.dim() != 3 or payload.shs.shape[0] != n or payload.shs.shape[2] != 3 or \
+                payload.shs.shape[1] < (deg + 1) ** 2:
+            return f"shs has shape {tuple(payload.shs.shape)}, expected [{n}, >= {(deg + 1) ** 2}, 3]"
+        for name in ("xyz", "opacities", "shs", "scales", "rotations", "target"):
+            t = getattr(payload, name)
+            if t.dtype != torch.float32:
+                return f"{name} is {t.dtype}, expected float32"
+            if not bool(torch.isfinite(t).all()):
+                return f"{name} holds non-finite values"
+    except (AttributeError, TypeError) as e:
+        return f"malformed request: {e}"
+    if solve_bytes(payload) > hbm_budget:
+        return f"needs {solve_bytes(payload) / 1e9:.3f} GB, above the HBM budget of {hbm_budget / 1e9:.3f} GB"
+    return ""
+
+
+def _is_oom(e: BaseException) -> bool:
+    return isinstance(e, torch.cuda.OutOfMemoryError) or (isinstance(e, RuntimeError) and "out of memory" in str(e))
 
 
 @dataclass
 class ServeStats:
     completed: list = field(default_factory=list)
+    refused: list = field(default_factory=list)  # rejected, cancelled and failed requests
     wall: float = 0.0
     admitted_peak: int = 0
     epochs: int = 0
@@ -140,6 +185,9 @@ class ServeStats:
         kinds = {k: [r for r in self.completed if r.kind == k] for k in ("pose", "render")}
         pl = np.array([r.latency for r in kinds["pose"]]) if kinds["pose"] else np.array([math.nan])
         return {"server": name, "completed": len(self.completed), "wall_s": round(self.wall, 3),
+                "rejected": sum(r.status == "rejected" for r in self.refused),
+                "cancelled": sum(r.status == "cancelled" for r in self.refused),
+                "failed": sum(r.status == "failed" for r in self.refused),
                 "throughput_req_s": round(len(self.completed) / self.wall, 4) if self.wall else None,
                 "pose_solves_per_s": round(len(kinds["pose"]) / self.wall, 4) if self.wall else None,
                 "renders_per_s": round(len(kinds["render"]) / self.wall, 4) if self.wall else None,
@@ -151,16 +199,42 @@ class ServeStats:
 
 
 class ContinuousBatchServer:
+    """Continuous batching of pose solves with renders on a side stream.
+
+    Failure handling, each confined to the request concerned (the other solves keep their
+    state and their results): a malformed request or one that could never fit the HBM
+    budget is rejected on arrival (validate_payload); cancel(rid) withdraws a queued
+    request, or an active solve at the next epoch boundary; a device allocation that
+    fails while a solve is admitted fails that request (the server carries on); a solve
+    whose pose turns non-finite is stopped at the next epoch boundary and failed (the
+    reference stops on a NaN loss, trainer/losses.py:126-127). `hooks` lets a caller
+    (tests) inject host-side faults: hooks["upload"](req) runs before a solve's inputs
+    are copied to the device (it may raise), hooks["epoch"](batch_solver, requests)
+    after every completed epoch."""
+
     def __init__(self, pose_payloads: list[PosePayload], render_targets: list[RenderTarget], device="cuda",
                  max_slots: int = 64, hbm_budget: float = 150e9, epoch: int = 25, iters: int = 300,
-                 use_graph: bool = True):
+                 use_graph: bool = True, hooks: dict | None = None):
         self.pose_payloads = pose_payloads
         self.render_targets = render_targets
         self.dev = torch.device(device)
         self.max_slots, self.hbm_budget, self.epoch, self.iters = max_slots, hbm_budget, epoch, iters
         self.use_graph = use_graph
+        self.hooks = dict(hooks or {})
+        self._cancel_lock = threading.Lock()
+        self._cancelled: set[int] = set()
         if iters % epoch:
             raise ValueError("iters must be a multiple of epoch")
+
+    def cancel(self, rid: int) -> None:
+        """Withdraws request `rid` (callable from any thread): dropped from the queue, or
+        stopped at the next epoch boundary if it is running."""
+        with self._cancel_lock:
+            self._cancelled.add(int(rid))
+
+    def _is_cancelled(self, rid: int) -> bool:
+        with self._cancel_lock:
+            return rid in self._cancelled
 
     def run(self, stream: list[Request], wall_limit: float = math.inf, stop_admitting_after: float = math.inf):
         """Serves `stream` (sorted by arrival) in real time from now. Stops when every
@@ -178,12 +252,17 @@ class ContinuousBatchServer:
         t0 = time.perf_counter()
         clock = lambda: time.perf_counter() - t0
 
+        def refuse(req, status, why):
+            req.status, req.error, req.done = status, why, clock()
+            stats.refused.append(req)
+
         def poll_renders():
             keep = []
             for req, ev, host in renders:
                 if ev.query():
                     req.done = clock()
                     req.result = float(host.double().sum())  # the image reached the host
+                    req.status = "ok"
                     pool.append(host)
                     stats.completed.append(req)
                 else:
@@ -194,8 +273,18 @@ class ContinuousBatchServer:
             now = clock()
             while pending and pending[0].arrival <= now:
                 r = pending.popleft()
-                if r.kind != "render":
-                    queue.append(r)
+                if r.kind == "pose":
+                    if not 0 <= r.payload < len(self.pose_payloads):
+                        refuse(r, "rejected", f"no pose payload {r.payload}")
+                        continue
+                    why = validate_payload(self.pose_payloads[r.payload], self.hbm_budget)
+                    if why:
+                        refuse(r, "rejected", why)
+                    else:
+                        queue.append(r)
+                    continue
+                if r.kind != "render" or not 0 <= r.payload < len(self.render_targets):
+                    refuse(r, "rejected", f"unknown request {r.kind} / {r.payload}")
                     continue
                 r.start = clock()
                 with torch.cuda.stream(rstream):
@@ -205,6 +294,19 @@ class ContinuousBatchServer:
                     ev = torch.cuda.Event()
                     ev.record(rstream)
                 renders.append((r, ev, host))
+
+        def drop(indices):
+            """Removes active solves `indices` (their requests are settled), keeping the
+            survivors' optimiser state."""
+            nonlocal used
+            if not indices:
+                return
+            if bs is not None and members == [id(x["req"]) for x in active]:
+                for s, a in enumerate(active):
+                    a["xi"], a["adam"] = bs.xi[s].clone(), bs.adam[s].clone()
+            for s in sorted(indices, reverse=True):
+                used -= active[s]["bytes"]
+                del active[s]
 
         while True:
             if clock() > wall_limit:
@@ -224,25 +326,34 @@ class ContinuousBatchServer:
                     continue
                 retries = 0
                 stats.epochs += 1
-                retired = []
+                if "epoch" in self.hooks:
+                    self.hooks["epoch"](bs, [a["req"] for a in active])
+                finite = torch.isfinite(bs.xi).all(dim=1).cpu().tolist()
+                gone = []
                 for s, a in enumerate(active):
                     a["it"] += self.epoch
-                    if a["it"] >= self.iters:
+                    if not finite[s]:
+                        refuse(a["req"], "failed", "the pose became non-finite (the loss diverged)")
+                        gone.append(s)
+                    elif self._is_cancelled(a["req"].rid):
+                        refuse(a["req"], "cancelled", f"cancelled after {a['it']} iterations")
+                        gone.append(s)
+                    elif a["it"] >= self.iters:
                         a["xi"], a["adam"] = bs.xi[s].clone(), bs.adam[s].clone()
                         a["req"].result = a["xi"].double().cpu().numpy()
                         a["req"].done = clock()
+                        a["req"].status = "ok"
                         stats.completed.append(a["req"])
-                        retired.append(s)
-                if retired:
-                    for s, a in enumerate(active):     # keep the survivors' optimiser state
-                        a["xi"], a["adam"] = bs.xi[s].clone(), bs.adam[s].clone()
-                    for s in reversed(retired):
-                        used -= active[s]["bytes"]
-                        del active[s]
+                        gone.append(s)
+                drop(gone)
             # epoch boundary: admission in arrival order, within slots and the HBM budget
             admitted = False
             while queue and len(active) < self.max_slots and clock() <= stop_admitting_after:
                 r = queue[0]
+                if self._is_cancelled(r.rid):
+                    queue.popleft()
+                    refuse(r, "cancelled", "cancelled while queued")
+                    continue
                 pl = self.pose_payloads[r.payload]
                 need = solve_bytes(pl)
                 if used + need > self.hbm_budget and active:
@@ -252,7 +363,18 @@ class ContinuousBatchServer:
                 if bs is not None and members == [id(a["req"]) for a in active]:
                     for s, a in enumerate(active):     # leaving the old batch: save its state
                         a["xi"], a["adam"] = bs.xi[s].clone(), bs.adam[s].clone()
-                active.append({"req": r, "prob": upload(pl, self.dev), "xi": torch.zeros(6, device=self.dev),
+                    members = None
+                try:
+                    if "upload" in self.hooks:
+                        self.hooks["upload"](r)
+                    prob = upload(pl, self.dev)
+                except Exception as e:
+                    if not _is_oom(e):
+                        raise
+                    refuse(r, "failed", f"device allocation failed: {e}")
+                    torch.cuda.empty_cache()
+                    continue
+                active.append({"req": r, "prob": prob, "xi": torch.zeros(6, device=self.dev),
                                "adam": torch.zeros(16, device=self.dev), "it": 0, "bytes": need})
                 used += need
                 admitted = True
@@ -298,6 +420,16 @@ class PlainFifoServer:
                 continue
             pending.popleft()
             r.start = clock()
+            why = ""
+            if r.kind == "pose":
+                why = validate_payload(self.pose_payloads[r.payload]) if 0 <= r.payload < len(self.pose_payloads) \
+                    else f"no pose payload {r.payload}"
+            elif r.kind != "render" or not 0 <= r.payload < len(self.render_targets):
+                why = f"unknown request {r.kind} / {r.payload}"
+            if why:
+                r.status, r.error, r.done = "rejected", why, clock()
+                stats.refused.append(r)
+                continue
             if r.kind == "render":
                 img = self.render_targets[r.payload].render()
                 r.result = img.cpu()
@@ -307,6 +439,7 @@ class PlainFifoServer:
                 r.result = xi
             torch.cuda.synchronize(self.dev)
             r.done = clock()
+            r.status = "ok"
             stats.completed.append(r)
             stats.admitted_peak = 1
         stats.wall = clock()

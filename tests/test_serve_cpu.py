@@ -56,3 +56,50 @@ def test_stats_summary_percentiles():
     assert s["peak_active_solves"] == 7
     empty = serve.ServeStats().summary("y")
     assert empty["completed"] == 0 and math.isnan(empty["latency_p50_s"])
+
+
+def _payload(n=500, h=18, w=32, deg=0):
+    from cfgs import scenes, serve
+    f = lambda *shape: torch.rand(*shape)
+    cam = scenes.make_camera(w, h, 30.0, 30.0)
+    return serve.PosePayload(f(n, 3), f(n, 1), f(n, (deg + 1) ** 2, 3), f(n, 3), f(n, 4), f(3, h, w), cam, deg)
+
+
+def test_validate_payload_rejects_malformed_and_oversized_requests():
+    """The server refuses, on arrival, what it could not serve; a well-formed request
+    passes. (CF-3DGS stops on a NaN loss, trainer/losses.py:126-127: NaN inputs are
+    refused up front.)"""
+    from cfgs import serve
+    ok = _payload()
+    assert serve.validate_payload(ok) == ""
+    cases = {
+        "xyz shape": lambda p: setattr(p, "xyz", torch.rand(p.xyz.shape[0], 2)),
+        "target size": lambda p: setattr(p, "target", torch.rand(3, 10, 10)),
+        "opacity count": lambda p: setattr(p, "opacities", torch.rand(3, 1)),
+        "sh width": lambda p: (setattr(p, "sh_degree", 2)),
+        "sh degree": lambda p: setattr(p, "sh_degree", 5),
+        "dtype": lambda p: setattr(p, "scales", p.scales.double()),
+        "nan": lambda p: p.xyz.__setitem__((3, 1), float("nan")),
+        "inf": lambda p: p.target.__setitem__((0, 0, 0), float("inf")),
+        "empty": lambda p: setattr(p, "xyz", torch.rand(0, 3)),
+        "missing": lambda p: setattr(p, "rotations", None),
+    }
+    for name, spoil in cases.items():
+        p = _payload()
+        spoil(p)
+        assert serve.validate_payload(p) != "", name
+    assert serve.validate_payload(ok, hbm_budget=serve.solve_bytes(ok)) == ""
+    why = serve.validate_payload(ok, hbm_budget=serve.solve_bytes(ok) - 1)
+    assert "HBM budget" in why
+
+
+def test_cancel_is_thread_safe_and_recorded():
+    import threading
+    from cfgs import serve
+    srv = serve.ContinuousBatchServer([], [], device="cpu", epoch=25, iters=300)
+    ts = [threading.Thread(target=srv.cancel, args=(i,)) for i in range(50)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert all(srv._is_cancelled(i) for i in range(50)) and not srv._is_cancelled(50)

@@ -70,3 +70,55 @@ def test_plain_fifo_server_runs(setup):
     st = serve.PlainFifoServer(payloads, targets, DEV, iters=ITERS).run(reqs)
     s = st.summary("plain")
     assert s["completed"] == 3 and s["latency_p99_s"] >= s["latency_p50_s"] > 0
+
+
+def test_failures_are_confined_to_their_requests(setup):
+    """Host-side fault injection (no device fault): a malformed request and one larger
+    than the HBM budget are rejected on arrival, a queued and a running solve are
+    cancelled, a simulated device allocation failure fails its request, and a solve
+    whose pose is poisoned with NaN mid-run is stopped and failed. Every other request
+    ends with the result it has alone."""
+    import copy
+    serve, pose, payloads, probs, targets = setup
+    from cfgs import scenes
+    bad = copy.copy(payloads[0])
+    bad.xyz = bad.xyz.clone()
+    bad.xyz[5, 1] = float("nan")
+    big_sc = scenes.scene_pose(width=256, height=144, seed=8)
+    big = serve.payload_from_problem(pose.make_problem(big_sc, DEV), big_sc.camera)
+    budget = 2 * max(serve.solve_bytes(p) for p in payloads)
+    assert serve.solve_bytes(big) > budget
+    pls = payloads + [bad, big]
+    kinds = [("pose", 0), ("pose", 4), ("pose", 1), ("pose", 2), ("pose", 5), ("pose", 3), ("render", 0),
+             ("pose", 1), ("pose", 0), ("render", 7)]
+    reqs = _stream(serve, kinds, spacing=0.0)
+    OOM_RID, NAN_RID, CANCEL_RUNNING, CANCEL_QUEUED = 3, 5, 2, 7
+    seen = {"epochs": 0}
+
+    def on_upload(req):
+        if req.rid == OOM_RID:
+            raise torch.cuda.OutOfMemoryError("simulated allocation failure")
+
+    def on_epoch(bs, active):
+        seen["epochs"] += 1
+        rids = [r.rid for r in active]
+        if seen["epochs"] == 2 and NAN_RID in rids:
+            bs.xi[rids.index(NAN_RID)] = float("nan")
+        if seen["epochs"] == 1:
+            srv.cancel(CANCEL_RUNNING)
+
+    srv = serve.ContinuousBatchServer(pls, targets, DEV, max_slots=3, hbm_budget=budget, epoch=EPOCH, iters=ITERS,
+                                      hooks={"upload": on_upload, "epoch": on_epoch})
+    srv.cancel(CANCEL_QUEUED)
+    st = srv.run(reqs)
+    status = {r.rid: r.status for r in reqs}
+    assert status == {0: "ok", 1: "rejected", 2: "cancelled", 3: "failed", 4: "rejected", 5: "failed",
+                      6: "ok", 7: "cancelled", 8: "ok", 9: "rejected"}, {r.rid: (r.status, r.error) for r in reqs}
+    assert "non-finite" in reqs[NAN_RID].error and "allocation" in reqs[OOM_RID].error
+    assert "HBM budget" in reqs[4].error
+    s = st.summary("x")
+    assert (s["completed"], s["rejected"], s["cancelled"], s["failed"]) == (3, 3, 2, 2)
+    want = pose.solve(probs[0], iters=ITERS, mode="fused")[0]
+    for rid in (0, 8):
+        assert np.array_equal(np.float32(reqs[rid].result), np.float32(want)), rid
+    assert reqs[6].result == float(targets[0].render().double().sum())
