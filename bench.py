@@ -60,6 +60,7 @@ def _args():
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-pose", action="store_true", help="skip the pose-solve half of the metric")
     p.add_argument("--no-tune", action="store_true", help="keep the default render schedule (no autotuning)")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
     p.add_argument("--workload", default="fwdbwd",
@@ -68,6 +69,15 @@ def _args():
     p.add_argument("--serve-seconds", type=float, default=60.0)
     p.add_argument("--serve-slots", type=int, default=64)
     return p.parse_args()
+
+
+def bench_config(sc, K: int, world: int) -> dict:
+    """The workload description both arms print (the same dict for the same workload)."""
+    D = (sc.sh_degree + 1) ** 2
+    return {"workload": f"{sc.n} SH{sc.sh_degree} Gaussians, {sc.camera.width}x{sc.camera.height}, "
+                        "fwd + L1 loss + bwd", "num_rendered": int(K),
+            "l2": f"inputs larger than L2 (Gaussian parameters {sc.n * (44 + 12 * D) / 1e6:.0f} MB)",
+            "parallelism": "replicas" if world > 1 else "1 GPU"}
 
 
 def _cores() -> int:
@@ -131,44 +141,58 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# algorithmic bytes per launch of each phase: the arrays each phase must read and write
-# once (N Gaussians, K instances, HW pixels, D SH coefficients)
+# Algorithmic bytes of one fwd + bwd iteration of the published algorithm, item by item
+# (N Gaussians, K tile instances, HW pixels, T tiles, D SH coefficients): the arrays it
+# must read and write once. Grouped by this build's phases; the binning group (12K
+# duplicate write + 24K one logical sort read+write + 8K + 8T ranges) covers the depth
+# sort and the instance binning together.
 # ---------------------------------------------------------------------------
-def phase_bytes(N: int, K: int, HW: int, D: int) -> dict:
-    params = N * (12 + 4 + 12 * D + 12 + 16)
+def phase_bytes(N: int, K: int, HW: int, D: int, T: int) -> dict:
+    params = N * (44 + 12 * D)
     return {
-        "preprocess": params + N * (8 + 16 + 16 + 8 + 4 + 1 + 4),
-        "depth_sort": N * (4 * 16 + 8),
-        "bin": N * (4 + 8 + 4 + 4) + K * (8 + 4) + K * (8 + 4 + 8),
-        "composite": K * (4 + 8 + 16 + 16) + HW * (12 + 4 + 4 + 4 + 4),
-        "render_bwd": K * (4 + 4 + 8 + 16 + 16 + 48) + HW * (4 + 4 + 12 + 4 + 4),
-        "preprocess_bwd": params + N * (4 + 4 + 1 + 4) + K * 48 + N * (12 + 12 + 4 + 12 + 24 + 12 * D + 12 + 16),
+        "preprocess": params + 48 * N + 8 * N,                 # parameters read, geometry write, scan
+        "binning": 12 * K + 24 * K + 8 * K + 8 * T,            # duplicate, sort, tile ranges
+        "composite": 44 * K + 28 * HW,
+        "render_bwd": 44 * K + 28 * HW + 36 * N,               # + the per-Gaussian 2D gradients written
+        "preprocess_bwd": N * (44 + 12 * D + 48 + 36) + N * (44 + 12 * D + 24),
     }
 
 
-# FP32 operations per (pixel, Gaussian) evaluation of the plain algorithm (an
-# exponential counted as one): forward ~11 + exp, backward ~40 + exp.
-ALU_OPS_PER_EVAL = {"composite": 12, "render_bwd": 41}
+# Bytes this build's render backward moves by design on top of the algorithm's: one
+# 48-byte gradient record per kept instance (written, then read by the preprocess
+# backward) and the one-byte written marks.
+def render_bwd_design_bytes(K: int, kept: int) -> int:
+    return 48 * kept + K
+
+
+# FP32 floating-point operations per plain-algorithm evaluation (E = sum of the per-pixel
+# contributor counts), counted with ncu (sm__sass_thread_inst_executed_op_{ffma,fadd,
+# fmul,ffma2,fadd2,fmul2}_pred_on.sum: FFMA 2, FADD/FMUL 1, FFMA2 4, FADD2/FMUL2 2 flops)
+# on the render kernels of a 250,000-Gaussian scene with the benchmark's distributions at
+# 1920x1080 (E = 634M): forward 5.24e9 and backward 8.46e9 flops per launch.
+FLOPS_PER_EVAL = {"composite": 5.24e9 / 633965142, "render_bwd": 8.46e9 / 633965142}
 
 
 def alu_roofline(E: int, phase_ms: dict, pb: dict, peaks: dict) -> dict:
-    """ALU roofline of the two render kernels: E = sum of the per-pixel contributor
-    counts (the evaluations of the plain per-pixel loop), E x ops per evaluation over the
-    kernel time against the nominal FP32 peak (SMs x 128 lanes x 2 flops x max clock;
-    no measured FP32 peak is available). Also the iteration's lower bound with each
-    phase at its tighter bound (bytes / HBM or ops / FP32) against the measured phases."""
+    """FP32 roofline of the two render kernels: E x counted flops per evaluation over the
+    kernel time against the nominal FP32 peak (SMs x 128 lanes x 2 flops x max clock; no
+    measured FP32 peak is available). Also the iteration's lower bound with each phase at
+    its tighter bound (bytes / HBM or flops / FP32) against the measured phases."""
     import torch
     props = torch.cuda.get_device_properties(0)
     mhz = peaks.get("sm_max_mhz") or 2070.0
     peak = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
-    out = {"E": E, "fp32_peak_tflops": round(peak, 2), "peak_source": "nominal (SMs x 128 x 2 x max clock)"}
+    out = {"E": E, "fp32_peak_tflops": round(peak, 2), "peak_source": "nominal (SMs x 128 x 2 x max clock)",
+           "flops_per_eval": {k: round(v, 3) for k, v in FLOPS_PER_EVAL.items()},
+           "flops_source": "ncu-counted FP32 instructions of the render kernels (250k-Gaussian scene, same "
+                           "distributions), per plain-algorithm evaluation"}
     t_min = 0.0
     for k, ms in phase_ms.items():
         t_hbm = pb[k] / (peaks["hbm_gbs"] * 1e9)
-        t_alu = E * ALU_OPS_PER_EVAL[k] / (peak * 1e12) if k in ALU_OPS_PER_EVAL else 0.0
+        t_alu = E * FLOPS_PER_EVAL[k] / (peak * 1e12) if k in FLOPS_PER_EVAL else 0.0
         t_min += max(t_hbm, t_alu)
-        if k in ALU_OPS_PER_EVAL:
-            tf = E * ALU_OPS_PER_EVAL[k] / (ms / 1000.0) / 1e12
+        if k in FLOPS_PER_EVAL:
+            tf = E * FLOPS_PER_EVAL[k] / (ms / 1000.0) / 1e12
             out[k] = {"achieved_tflops": round(tf, 3), "frac": round(tf / peak, 4)}
     out["iteration_bound_ms"] = round(t_min * 1000.0, 4)
     out["iteration_frac"] = round(t_min * 1000.0 / sum(phase_ms.values()), 4)
@@ -275,18 +299,26 @@ def run_ours(a) -> None:
 
     phase_ms = {k: sum(s_.elapsed_time(e_) for s_, e_ in v) / len(v) for k, v in timers.items()}
     D = (sc.sh_degree + 1) ** 2
-    pb = phase_bytes(sc.n, K, HW, D)
-    dom = max(phase_ms, key=phase_ms.get)
+    T = ((cam.width + 15) // 16) * ((cam.height + 15) // 16)
+    pb = phase_bytes(sc.n, K, HW, D, T)
+    group_ms = {"preprocess": phase_ms["preprocess"], "binning": phase_ms["depth_sort"] + phase_ms["bin"],
+                "composite": phase_ms["composite"], "render_bwd": phase_ms["render_bwd"],
+                "preprocess_bwd": phase_ms["preprocess_bwd"]}
+    dom = max(group_ms, key=group_ms.get)
     peaks = _peaks()
-    achieved = pb[dom] / (phase_ms[dom] / 1000.0) / 1e9
+    achieved = pb[dom] / (group_ms[dom] / 1000.0) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 5),
                 "peak_source": peaks["source"], "traffic": _traffic(dom, K),
-                "algorithmic_bytes_per_launch": pb[dom]}
-    phases = {k: {"ms": round(v, 4), "share": round(v / sum(phase_ms.values()), 4),
-                  "hbm_frac": round(pb[k] / (v / 1000.0) / 1e9 / peaks["hbm_gbs"], 5)} for k, v in phase_ms.items()}
+                "algorithmic_bytes_per_launch": pb[dom],
+                "note": "algorithmic bytes of the published algorithm for this kernel; the kernel is bound by "
+                        "instruction issue, see render_alu"}
+    phases = {k: {"ms": round(v, 4), "share": round(v / sum(phase_ms.values()), 4)} for k, v in phase_ms.items()}
+    hbm_groups = {k: {"ms": round(v, 4), "algorithmic_bytes": pb[k],
+                      "hbm_frac": round(pb[k] / (v / 1000.0) / 1e9 / peaks["hbm_gbs"], 5)} for k, v in group_ms.items()}
+    iter_bytes = sum(pb.values())
     E = int(raster.inspect_state(last_state[0], cam.width, cam.height)["n_contrib"].to(torch.int64).sum())
-    render_alu = alu_roofline(E, phase_ms, pb, peaks)
+    render_alu = alu_roofline(E, group_ms, pb, peaks)
 
     e2e = None
     if not a.no_e2e:
@@ -296,20 +328,26 @@ def run_ours(a) -> None:
     if rank == 0 and not a.no_cpu:
         cpu = run_cpu_baseline(sc, a.cpu_budget_s)
 
+    pose_suite = None
+    if rank == 0 and not a.no_pose:
+        pose_suite = run_pose_suite(a, dev)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{sc.n} SH{sc.sh_degree} Gaussians, {a.width}x{a.height}, "
-                                   f"fwd + L1 loss + bwd", "num_rendered": int(K),
-                       "render_schedule": {"fwd_batch": sched.fwd_batch, "fwd_warps": sched.fwd_warps,
-                                           "bwd_batch": sched.bwd_batch},
-                       "l2": "inputs larger than L2 (Gaussian parameters "
-                             f"{sc.n * (44 + 12 * D) / 1e6:.0f} MB)", "parallelism": "replicas" if world > 1 else "1 GPU"},
-            "roofline": roofline, "phases": phases, "render_alu": render_alu, "cpu_baseline": cpu, "e2e": e2e,
+            "config": bench_config(sc, K, world),
+            "render_schedule": {"fwd_batch": sched.fwd_batch, "fwd_warps": sched.fwd_warps,
+                                "bwd_batch": sched.bwd_batch},
+            "roofline": roofline, "phases": phases, "hbm_by_phase": hbm_groups,
+            "iteration_hbm": {"algorithmic_bytes": iter_bytes,
+                              "achieved_gbs": round(iter_bytes / (ms_per_step / 1000.0) / 1e9, 2),
+                              "frac": round(iter_bytes / (ms_per_step / 1000.0) / 1e9 / peaks["hbm_gbs"], 5)},
+            "render_alu": render_alu, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk,
             "gpu_launches": (raster.kernel_launches(sc.camera.width, sc.camera.height)["total"] + 2) * a.steps,
+            "pose": pose_suite,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -455,10 +493,10 @@ def run_reference(a) -> None:
     cores = _cores()
     c_oracle.set_threads(cores)
     sc = scenes.scene_large(n=a.n, width=a.width, height=a.height, seed=1)
-    t_w = 0.0
+    t_w, K = 0.0, 0
     for _ in range(max(a.warmup, 1)):
         t0 = time.perf_counter()
-        _oracle_iteration(sc, c_oracle.Oracle)
+        K = _oracle_iteration(sc, c_oracle.Oracle)
         t_w = time.perf_counter() - t0
     # a rate: when the requested steps would run past ~150 s, time fewer of them
     steps = max(1, min(a.steps, int(150.0 / max(t_w, 1e-3))))
@@ -471,7 +509,7 @@ def run_reference(a) -> None:
         "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1000 * dt / steps, 2), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{sc.n} SH{sc.sh_degree} Gaussians, {a.width}x{a.height}, fwd + L1 loss + bwd"},
+        "config": bench_config(sc, K, int(os.environ.get("WORLD_SIZE", "1"))),
         "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"each step one full fwd+bwd iteration ({steps} of {a.steps} steps timed)"},
         "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -493,27 +531,28 @@ def _pose_setup(dev, count, seed=3):
     return specs, probs, cams
 
 
-def run_pose(a) -> None:
-    """One CF-3DGS relative-pose solve (640x360, one Gaussian per pixel, 300 Adam
-    iterations, lr 1e-3, RGB L1), end to end per solve: the plain path (PyTorch pose
-    algebra + autograd + torch Adam around the rasteriser), the fused pose kernels behind
-    autograd, and the solve engine (one launch per stage, CUDA-graph replays, no host
-    synchronisation inside the 300 iterations; its setup is inside the timed region)."""
-    import time
+def _pct(x, q):
     import numpy as np
+    return round(float(np.percentile(np.asarray(x, np.float64), q)), 4)
+
+
+def pose_single(dev, engine_reps: int = 5, plain_reps: int = 2) -> dict:
+    """One CF-3DGS relative-pose solve (640x360, one Gaussian per pixel, 300 Adam
+    iterations, lr 1e-3, RGB L1; trainer/cf3dgs_trainer.py:261-285), end to end per
+    solve: the plain path (PyTorch pose algebra + autograd + torch Adam around the
+    rasteriser: the reference's structure), the fused pose kernels behind autograd, and
+    the solve engine (batched kernels, CUDA-graph replays, no host synchronisation inside
+    the 300 iterations; its setup inside the timed region)."""
     import torch
     import diff_gaussian_rasterization  # noqa: F401
-    from cfgs import batch, pose, scenes
-    dev = torch.device("cuda", 0)
+    from cfgs import autotune, batch, pose, scenes
     prob = pose.make_problem(scenes.scene_pose(width=640, height=360, seed=2), dev)
     res = {}
-    for mode in ("plain", "fused"):
+    for mode, reps in (("plain", plain_reps), ("fused", plain_reps)):
         pose.time_solves(prob, mode, count=1)
-        sps, lat = pose.time_solves(prob, mode, count=max(2, a.steps // 5))
+        sps, lat = pose.time_solves(prob, mode, count=reps)
         xi, _ = pose.solve(prob, mode=mode)
-        res[mode] = {"solves_per_s": round(sps, 4), "latency_s": [round(x, 4) for x in lat], "xi": xi}
-
-    from cfgs import autotune
+        res[mode] = {"solves_per_s": sps, "latency_s": lat, "xi": xi}
     tuner = autotune.Autotuner()
 
     def engine_solve():
@@ -521,29 +560,38 @@ def run_pose(a) -> None:
 
     engine_solve()
     lat = []
-    for _ in range(max(3, a.steps // 2)):
+    for _ in range(engine_reps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         xi = engine_solve()
         torch.cuda.synchronize()
         lat.append(time.perf_counter() - t0)
-    res["engine"] = {"solves_per_s": round(len(lat) / sum(lat), 4), "latency_s": [round(x, 4) for x in lat], "xi": xi}
     dang, dtr = pose.pose_error(res["plain"]["xi"], res["fused"]["xi"])
-    eang, etr = pose.pose_error(res["plain"]["xi"], res["engine"]["xi"])
-    gerr = pose.pose_error(res["engine"]["xi"], prob.xi_gt)
-    line = {"metric": "pose solves/s (640x360, 300 iterations)", "value": res["engine"]["solves_per_s"],
-            "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "CF-3DGS relative pose solve, 230400 SH0 Gaussians, 640x360, 300 Adam iters",
-                       "path": "solve engine (cfgs_batch_iteration, CUDA graphs), setup included",
-                       "render_schedule": str(autotune.get_schedule())},
-            "latency_p50_s": round(float(np.percentile(lat, 50)), 4),
-            "latency_p99_s": round(float(np.percentile(lat, 99)), 4),
-            "plain_solves_per_s": res["plain"]["solves_per_s"],
-            "fused_autograd_solves_per_s": res["fused"]["solves_per_s"],
-            "speedup_vs_plain": round(res["engine"]["solves_per_s"] / res["plain"]["solves_per_s"], 3),
+    eang, etr = pose.pose_error(res["plain"]["xi"], xi)
+    gerr = pose.pose_error(xi, prob.xi_gt)
+    sps = len(lat) / sum(lat)
+    return {"workload": "CF-3DGS relative pose solve, 230400 SH0 Gaussians, 640x360, 300 Adam iterations, RGB L1",
+            "solves_per_s": round(sps, 4), "latency_p50_s": _pct(lat, 50), "latency_p99_s": _pct(lat, 99),
+            "solves_timed": len(lat),
+            "plain_solves_per_s": round(res["plain"]["solves_per_s"], 4),
+            "plain_latency_p50_s": _pct(res["plain"]["latency_s"], 50),
+            "plain_latency_p99_s": _pct(res["plain"]["latency_s"], 99),
+            "fused_autograd_solves_per_s": round(res["fused"]["solves_per_s"], 4),
+            "speedup_vs_plain": round(sps / res["plain"]["solves_per_s"], 3),
             "plain_vs_fused": {"rot_deg": dang, "trans": dtr},
             "plain_vs_engine": {"rot_deg": eang, "trans": etr},
-            "engine_vs_ground_truth": {"rot_deg": gerr[0], "trans": gerr[1]}}
+            "engine_vs_ground_truth": {"rot_deg": gerr[0], "trans": gerr[1]},
+            "path": "solve engine (cfgs_batch_iteration in CUDA graphs), setup included",
+            "render_schedule": str(autotune.get_schedule())}
+
+
+def run_pose(a) -> None:
+    import torch
+    dev = torch.device("cuda", 0)
+    r = pose_single(dev, engine_reps=max(3, a.steps // 2), plain_reps=max(2, a.steps // 5))
+    line = {"metric": "pose solves/s (640x360, 300 iterations)", "value": r["solves_per_s"], "unit": "solves/s",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": r["workload"], "path": r["path"]}, **r}
     print(json.dumps(line), flush=True)
 
 
@@ -576,43 +624,74 @@ def run_pose_iter(a) -> None:
                                  "instance_capacity": int(K0)}}), flush=True)
 
 
-def run_batch(a) -> None:
+def pose_batch(dev, probs, sample: int = 8) -> dict:
     """64 pose solves (N log-uniform in [5e4, 5e5], resolutions 320x180/640x360/960x540)
-    batched in one launch per stage with CUDA-graph replays, vs the same solves one by one
-    on the plain path (timed on a sample of them)."""
+    batched (one launch per stage, CUDA-graph replays) vs the same solves one after
+    another on the plain path, timed on the first `sample` of them."""
     import numpy as np
-    import torch
     from cfgs import batch, pose
-    dev = torch.device("cuda", 0)
-    specs, probs, _ = _pose_setup(dev, 64)
     bs = batch.BatchSolver(probs, autotune=True)
     bs.solve(300)  # tunes the render schedule for this batch shape (cached), untimed
     r = bs.solve(300)
-    sample = max(2, min(8, a.steps))
     batch.solve_sequential(probs[:1], 300, "plain")
     xs, lat = batch.solve_sequential(probs[:sample], 300, "plain")
     plain_sps = sample / sum(lat)
     xf, latf = batch.solve_sequential(probs[:sample], 300, "fused")
     agree = [pose.pose_error(xs[i], r.xi[i]) for i in range(sample)]
-    line = {"metric": "batched pose solves/s (64 uneven solves)", "value": round(64 / r.seconds, 4),
-            "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "64 CF-3DGS pose solves, N log-uniform [5e4,5e5], 3 resolutions, 300 iters",
-                       "total_gaussians": int(sum(p.xyz.shape[0] for p in probs)), "num_rendered": r.num_rendered0,
-                       "graph_chunk": bs.graph_chunk, "render_schedule": str(bs.schedule)},
-            "batch_seconds": round(r.seconds, 3), "ms_per_iteration": round(1000 * r.seconds / 300, 3),
+    sps = len(probs) / r.seconds
+    return {"workload": f"{len(probs)} CF-3DGS pose solves, N log-uniform [5e4,5e5], 320x180/640x360/960x540, "
+                        "300 Adam iterations each",
+            "solves_per_s": round(sps, 4), "batch_seconds": round(r.seconds, 3),
+            "latency_s": round(r.seconds, 3),
+            "ms_per_iteration": round(1000 * r.seconds / 300, 3),
+            "total_gaussians": int(sum(p.xyz.shape[0] for p in probs)), "num_rendered": r.num_rendered0,
             "plain_sequential_solves_per_s": round(plain_sps, 4), "plain_sample": sample,
+            "plain_latency_p50_s": _pct(lat, 50), "plain_latency_p99_s": _pct(lat, 99),
             "fused_sequential_solves_per_s": round(sample / sum(latf), 4),
-            "speedup_vs_plain": round((64 / r.seconds) / plain_sps, 3),
+            "speedup_vs_plain": round(sps / plain_sps, 3),
             "batched_vs_fused_single_bit_identical": bool(np.array_equal(np.float32(xf), np.float32(r.xi[:sample]))),
-            "batched_vs_plain_max": {"rot_deg": max(x[0] for x in agree), "trans": max(x[1] for x in agree)}}
+            "batched_vs_plain_max": {"rot_deg": max(x[0] for x in agree), "trans": max(x[1] for x in agree)},
+            "graph_chunk": bs.graph_chunk, "render_schedule": str(bs.schedule)}
+
+
+def run_batch(a) -> None:
+    import torch
+    dev = torch.device("cuda", 0)
+    _, probs, _ = _pose_setup(dev, 64)
+    r = pose_batch(dev, probs, sample=max(2, min(8, a.steps)))
+    line = {"metric": "batched pose solves/s (64 uneven solves)", "value": r["solves_per_s"], "unit": "solves/s",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": r["workload"]}, **r}
     print(json.dumps(line), flush=True)
 
 
+def pose_serve(dev, payloads, target, rate: float, seconds: float, plain_seconds: float, slots: int = 64,
+               seed: int = 11) -> dict:
+    """A Poisson stream of `rate` req/s (90% pose solves of the 64-solve mix, 10% renders
+    of a device-resident 1M-Gaussian SH3 scene at 1920x1080) served by the
+    continuous-batching server for `seconds` and by the plain FIFO loop for
+    `plain_seconds` (requests still queued or running at the end are not counted)."""
+    from cfgs import serve
+    out = {}
+    for name, secs in (("continuous", seconds), ("plain_fifo", plain_seconds)):
+        stream = serve.poisson_stream(rate, secs, 0.9, len(payloads), 1, seed=seed)
+        if name == "continuous":
+            srv = serve.ContinuousBatchServer(payloads, [target], dev, max_slots=slots, hbm_budget=150e9)
+        else:
+            srv = serve.PlainFifoServer(payloads, [target], dev)
+        st = srv.run(stream, wall_limit=secs)
+        s = st.summary(name)
+        s["arrived"] = len(stream)
+        s["stream_seconds"] = secs
+        out[name] = s
+    c, p = out["continuous"], out["plain_fifo"]
+    return {"workload": f"Poisson {rate:g} req/s, 90% pose solves (64-solve mix), 10% renders of 1M SH3 Gaussians "
+                        "at 1920x1080", "hbm_budget_gb": 150, "max_slots": slots, "epoch_iterations": 25,
+            "continuous": c, "plain_fifo": p,
+            "pose_throughput_speedup_vs_plain": round(c["pose_solves_per_s"] / max(p["pose_solves_per_s"], 1e-9), 3)}
+
+
 def run_serve(a) -> None:
-    """A Poisson stream (rate a.serve_rate req/s for a.serve_seconds s; 90% pose solves of
-    the 64-solve mix, 10% renders of a device-resident 1M-Gaussian SH3 scene at
-    1920x1080) served by the continuous-batching server and by a plain FIFO loop, each
-    for the length of the stream."""
     import torch
     from cfgs import scenes, serve
     dev = torch.device("cuda", 0)
@@ -622,26 +701,39 @@ def run_serve(a) -> None:
     target = serve.RenderTarget(scenes.scene_large(), dev)
     target.render()
     torch.cuda.synchronize()
-    out = {}
-    for name in ("continuous", "plain_fifo"):
-        stream = serve.poisson_stream(a.serve_rate, a.serve_seconds, 0.9, len(payloads), 1, seed=11)
-        if name == "continuous":
-            srv = serve.ContinuousBatchServer(payloads, [target], dev, max_slots=a.serve_slots, hbm_budget=150e9)
-        else:
-            srv = serve.PlainFifoServer(payloads, [target], dev)
-        st = srv.run(stream, wall_limit=a.serve_seconds)
-        s = st.summary(name)
-        s["arrived"] = len(stream)
-        out[name] = s
-    c, p = out["continuous"], out["plain_fifo"]
-    line = {"metric": "served requests/s (90% pose solves, 10% 1080p renders)", "value": c["throughput_req_s"],
-            "unit": "req/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"Poisson {a.serve_rate} req/s for {a.serve_seconds} s, 90% pose solves "
-                                   "(64-solve mix), 10% renders of 1M SH3 Gaussians at 1920x1080",
-                       "hbm_budget_gb": 150, "max_slots": a.serve_slots, "epoch_iterations": 25},
-            "continuous": c, "plain_fifo": p,
-            "pose_throughput_speedup_vs_plain": round(c["pose_solves_per_s"] / max(p["pose_solves_per_s"], 1e-9), 3)}
+    r = pose_serve(dev, payloads, target, a.serve_rate, a.serve_seconds, a.serve_seconds, a.serve_slots)
+    line = {"metric": "served requests/s (90% pose solves, 10% 1080p renders)",
+            "value": r["continuous"]["throughput_req_s"], "unit": "req/s", "n_gpus": 1, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic", "config": {"workload": r["workload"]}, **r}
     print(json.dumps(line), flush=True)
+
+
+def run_pose_suite(a, dev) -> dict:
+    """The metric's second half, measured in the default run: solves/s and latency of
+    the pose-solve workloads against the plain path, with the clocks of their timed
+    regions. One 640x360 solve; the 64-solve batch (plain timed on 8 of them); the served
+    stream at 200 req/s (continuous server for 60 s, plain FIFO for 20 s: both are
+    saturated, so the shorter window gives the plain loop's rate) and at a rate the
+    continuous server sustains (8 req/s, 20 s each), for latencies without a standing
+    queue."""
+    import torch
+    from cfgs import scenes, serve
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    out = {"single": pose_single(dev)}
+    _, probs, cams = _pose_setup(dev, 64)
+    out["batch64"] = pose_batch(dev, probs, sample=8)
+    payloads = [serve.payload_from_problem(p, c) for p, c in zip(probs, cams)]
+    del probs
+    torch.cuda.empty_cache()
+    target = serve.RenderTarget(scenes.scene_large(), dev)
+    target.render()
+    torch.cuda.synchronize()
+    out["served_200"] = pose_serve(dev, payloads, target, a.serve_rate, a.serve_seconds, min(20.0, a.serve_seconds),
+                                   a.serve_slots)
+    out["served_sustained"] = pose_serve(dev, payloads, target, 8.0, 20.0, 20.0, a.serve_slots, seed=12)
+    out["clocks"] = clocks.stop()
+    return out
 
 
 def run_ssim(a) -> None:

@@ -8,7 +8,9 @@ instance (streams created by torch are valid in the library).
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -53,23 +55,48 @@ def _compile(nvcc: str, src: str, extra: list[str]) -> Path:
     return obj
 
 
-def _stale() -> bool:
-    if not LIB_PATH.exists():
-        return True
-    t = LIB_PATH.stat().st_mtime
-    deps = [SRC_DIR / s for s in SOURCES] + list(SRC_DIR.glob("*.cuh")) + list(INCLUDE_DIR.glob("*.h"))
+STAMP_PATH = LIB_DIR / "libcfgs.stamp"
+
+
+def _fingerprint(nvcc: str | None, extra: list[str]) -> str:
+    """Hash of everything the library is built from: every source and header, this
+    recipe, the flags, the compiler's version line and the host architecture. A library
+    whose stamp differs (edited sources, other flags, a copy built on another machine) is
+    rebuilt, whatever the files' modification times say."""
+    h = hashlib.sha256()
+    deps = [SRC_DIR / s for s in SOURCES] + sorted(SRC_DIR.glob("*.cuh")) + sorted(INCLUDE_DIR.glob("*.h"))
     deps.append(Path(__file__))
-    return any(p.stat().st_mtime > t for p in deps if p.exists())
+    for p in deps:
+        h.update(p.name.encode())
+        h.update(p.read_bytes() if p.exists() else b"<missing>")
+    h.update(repr((COMMON_FLAGS, ARCH_FLAGS, sorted(NO_CONTRACT), extra)).encode())
+    h.update(platform.machine().encode())
+    if nvcc:
+        try:
+            out = subprocess.run([nvcc, "--version"], capture_output=True, text=True).stdout
+            h.update(out.strip().splitlines()[-1].encode() if out.strip() else b"")
+        except OSError:
+            pass
+    return h.hexdigest()
+
+
+def _stale(fingerprint: str) -> bool:
+    if not LIB_PATH.exists() or not STAMP_PATH.exists():
+        return True
+    return STAMP_PATH.read_text().strip() != fingerprint
 
 
 def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
-    """Compiles (if stale) and returns the path of libcfgs.so."""
-    if not force and not _stale():
+    """Compiles (when the library's stamp does not match its sources, flags and
+    toolchain) and returns the path of libcfgs.so."""
+    extra = list(extra_flags or [])
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    fp = _fingerprint(nvcc if Path(nvcc).exists() else None, extra)
+    if not force and not _stale(fp):
         return LIB_PATH
     nvcc = _nvcc()
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
     LIB_DIR.mkdir(parents=True, exist_ok=True)
-    extra = list(extra_flags or [])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s, extra), SOURCES))
     tmp = LIB_PATH.with_suffix(".so.tmp")
@@ -80,6 +107,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB_PATH)
+    STAMP_PATH.write_text(fp + "\n")
     if verbose:
         print(f"built {LIB_PATH}", file=sys.stderr)
     return LIB_PATH

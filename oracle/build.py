@@ -6,7 +6,9 @@ and per-tile loops (the results do not depend on the thread count).
 """
 from __future__ import annotations
 
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -21,10 +23,27 @@ FLAGS = ["-O2", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-sh
          "-Wno-unknown-pragmas"]
 
 
+STAMP = OUT_DIR / "libcfgs_oracle.stamp"
+
+
+def _fingerprint(cc: str | None) -> str:
+    """Hash of the sources, this recipe, the flags, the compiler and the host
+    architecture; the library is rebuilt whenever its stamp differs."""
+    h = hashlib.sha256()
+    for p in SRCS + [Path(__file__)]:
+        h.update(p.name.encode())
+        h.update(p.read_bytes())
+    h.update(repr(FLAGS).encode())
+    h.update(platform.machine().encode())
+    h.update((cc or "").encode())
+    return h.hexdigest()
+
+
 def build(force: bool = False) -> Path:
-    if not force and LIB.exists() and LIB.stat().st_mtime >= max([p.stat().st_mtime for p in SRCS] + [Path(__file__).stat().st_mtime]):
-        return LIB
     cc = shutil.which("gcc") or shutil.which("cc")
+    fp = _fingerprint(cc)
+    if not force and LIB.exists() and STAMP.exists() and STAMP.read_text().strip() == fp:
+        return LIB
     if cc is None:
         raise RuntimeError("no C compiler found for the oracle")
     OUT_DIR.mkdir(parents=True, exist_ok=True)
@@ -34,6 +53,7 @@ def build(force: bool = False) -> Path:
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    STAMP.write_text(fp + "\n")
     return LIB
 
 
