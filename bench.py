@@ -62,9 +62,10 @@ def _args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-pose", action="store_true", help="skip the pose-solve half of the metric")
     p.add_argument("--no-tune", action="store_true", help="keep the default render schedule (no autotuning)")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain GPU path's iteration")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
     p.add_argument("--workload", default="fwdbwd",
-                   choices=["fwdbwd", "pose", "pose_iter", "batch", "serve", "ssim", "init", "optim"])
+                   choices=["fwdbwd", "plain", "pose", "pose_iter", "batch", "serve", "ssim", "init", "optim"])
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--serve-seconds", type=float, default=60.0)
     p.add_argument("--serve-slots", type=int, default=64)
@@ -320,6 +321,10 @@ def run_ours(a) -> None:
     E = int(raster.inspect_state(last_state[0], cam.width, cam.height)["n_contrib"].to(torch.int64).sum())
     render_alu = alu_roofline(E, group_ms, pb, peaks)
 
+    plain_gpu = None
+    if rank == 0 and not a.no_plain:
+        plain_gpu = run_plain_gpu(a, rs, s, target, K, value / world)
+
     e2e = None
     if not a.no_e2e:
         e2e = run_e2e(a, dgr, sc, rs, dev, barrier, world)
@@ -344,7 +349,7 @@ def run_ours(a) -> None:
             "iteration_hbm": {"algorithmic_bytes": iter_bytes,
                               "achieved_gbs": round(iter_bytes / (ms_per_step / 1000.0) / 1e9, 2),
                               "frac": round(iter_bytes / (ms_per_step / 1000.0) / 1e9 / peaks["hbm_gbs"], 5)},
-            "render_alu": render_alu, "cpu_baseline": cpu, "e2e": e2e,
+            "render_alu": render_alu, "plain_gpu": plain_gpu, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk,
             "gpu_launches": (raster.kernel_launches(sc.camera.width, sc.camera.height)["total"] + 2) * a.steps,
             "pose": pose_suite,
@@ -352,6 +357,80 @@ def run_ours(a) -> None:
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_plain_gpu(a, rs, s, target, K: int, ours_value: float) -> dict:
+    """The same iteration on the plain GPU path (cfgs.plain: the published rasteriser's
+    structure, 64-bit keys and one radix sort, one thread per pixel, global atomic
+    gradients), with the loss as the reference trainer forms it (autograd of the L1 of
+    the clamped render, utils/loss_utils.py:15 with scene/gaussian_model_cf.py:885). The
+    reference's own CUDA rasteriser is an un-vendored submodule, so this is the GPU
+    comparison point for the tuned path on the same device."""
+    import torch
+    from cfgs import plain
+
+    timers: dict = {}
+    cap = [K]  # the instance buffers are sized for the count the last call saw, as upstream keeps its buffers
+
+    def step(tm=None):
+        color, radii, depth, alpha, st = plain.forward(rs, s.means3D, s.opacities, s.shs, None, s.scales,
+                                                       s.rotations, None, timers=tm, capacity_hint=cap[0])
+        cap[0] = st.capacity
+        ev = None
+        if tm is not None:
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record()
+        c = color.detach().requires_grad_(True)
+        loss = (c.clamp(0.0, 1.0) - target).abs().mean()
+        (g,) = torch.autograd.grad(loss, c)
+        if ev is not None:
+            ev[1].record()
+            tm.setdefault("loss", []).append(ev)
+        plain.backward(rs, st, s.means3D, s.opacities, s.shs, None, s.scales, s.rotations, None, g, None, None,
+                       timers=tm)
+        return st
+
+    for _ in range(max(a.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(3, a.steps)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(steps):
+        st = step(timers)
+    t1.record()
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / steps
+    phases = {k: round(sum(a_.elapsed_time(b_) for a_, b_ in v) / len(v), 4) for k, v in timers.items()}
+    value = 1000.0 / ms
+    return {"value": round(value, 4), "unit": UNIT, "ms_per_step": round(ms, 4), "steps": steps,
+            "num_rendered": st.num_rendered, "phases_ms": phases,
+            "ours_over_plain": round(ours_value / value, 3),
+            "what": "reference CUDA rasteriser not available (un-vendored submodule): the build's plain GPU path, "
+                    "the published rasteriser's structure (include/cfgs_plain.h), same preprocess and per-Gaussian "
+                    "backward kernels, loss by torch autograd as the reference trainer forms it"}
+
+
+def run_plain(a) -> None:
+    """Only the plain GPU path's iteration on the benchmarked workload (for profiling it
+    alone); one JSON line."""
+    import torch
+    import diff_gaussian_rasterization as dgr
+    from cfgs import scenes
+    dev = torch.device("cuda", 0)
+    sc = scenes.scene_large(n=a.n, width=a.width, height=a.height, seed=1)
+    cam = sc.camera.to(dev)
+    rs = dgr.GaussianRasterizationSettings(cam.height, cam.width, cam.tanfovx, cam.tanfovy, sc.bg.to(dev), 1.0,
+                                           cam.viewmatrix, cam.projmatrix, sc.sh_degree, cam.campos, False, False)
+    s = sc.to(dev)
+    r = run_plain_gpu(a, rs, s, s.target, 1, 1.0)
+    r.pop("ours_over_plain")
+    line = {"metric": METRIC, "value": r.pop("value"), "unit": UNIT, "n_gpus": 1, "steps": r.pop("steps"),
+            "warmup": a.warmup, "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": f"{sc.n} SH{sc.sh_degree} Gaussians, {cam.width}x{cam.height}, "
+                                                         "fwd + L1 loss + bwd, plain GPU path"}, **r}
+    print(json.dumps(line), flush=True)
 
 
 def run_e2e(a, dgr, sc, rs, dev, barrier, world) -> dict:
@@ -978,6 +1057,8 @@ def main():
     a = _args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "plain":
+        run_plain(a)
     elif a.workload == "pose":
         run_pose(a)
     elif a.workload == "pose_iter":

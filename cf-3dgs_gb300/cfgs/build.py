@@ -28,8 +28,8 @@ COMMON_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcomp
                 "--expt-relaxed-constexpr", f"-I{INCLUDE_DIR}"]
 # Translation units whose float results the CPU oracle reproduces bit for bit are
 # compiled without FMA contraction; their fused operations are explicit fmaf() calls.
-NO_CONTRACT = {"preprocess.cu", "render_fwd.cu"}
-SOURCES = ["preprocess.cu", "binning.cu", "render_fwd.cu", "render_bwd.cu", "preprocess_bwd.cu", "pose.cu", "batch.cu", "ssim.cu", "pointcloud.cu", "densify.cu", "loss.cu"]
+NO_CONTRACT = {"preprocess.cu", "render_fwd.cu", "plain_raster.cu"}
+SOURCES = ["preprocess.cu", "binning.cu", "render_fwd.cu", "render_bwd.cu", "preprocess_bwd.cu", "pose.cu", "batch.cu", "ssim.cu", "pointcloud.cu", "densify.cu", "loss.cu", "plain_raster.cu"]
 
 
 def _nvcc() -> str:

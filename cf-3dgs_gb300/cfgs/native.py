@@ -151,6 +151,13 @@ EXPORTS = {
     "cfgs_ssim_backward": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cfgs_render_schedule_check": (C.c_int, [C.POINTER(RenderSchedule), C.POINTER(RenderSchedule)]),
     "cfgs_diag_copy_timeout": (C.c_int, [C.c_uint32, _vp, _vp]),
+    # include/cfgs_plain.h: the plain GPU path (published structure, comparison point)
+    "cfgs_plain_work_bytes": (C.c_size_t, [C.c_int32, C.c_int64, C.c_int32, C.c_int32]),
+    "cfgs_plain_bin": (C.c_int, [C.POINTER(Settings), C.c_int32, _vp, _vp, C.c_int64, C.POINTER(C.c_int64), _vp]),
+    "cfgs_plain_render_forward": (C.c_int, [C.POINTER(Settings), C.c_int32, _vp, _vp, _vp, C.c_int64, _vp, _vp, _vp,
+                                            _vp]),
+    "cfgs_plain_backward": (C.c_int, [C.POINTER(Settings), C.POINTER(Gaussians), _vp, _vp, _vp, _vp, C.c_int64, _vp,
+                                      _vp, _vp, C.POINTER(Gradients), _vp]),
     "cfgs_l1_loss_scratch_bytes": (C.c_size_t, [C.c_int64]),
     "cfgs_l1_loss_forward": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, _vp, _vp]),
     "cfgs_l1_loss_backward": (C.c_int, [C.c_int64, _vp, _vp, C.c_int32, _vp, _vp, _vp]),

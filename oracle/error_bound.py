@@ -108,10 +108,33 @@ def _dot3(a, b):
     return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]
 
 
-def backward_bounds(o) -> dict:
+def contribution_counts(o) -> np.ndarray:
+    """Per Gaussian, the number of (pixel, instance) pairs of the oracle's forward `o`
+    that the backward visits: instance positions below the pixel's contributor count.
+    An upper bound on the terms one Gaussian's gradient sums add up."""
+    out = np.zeros(o.N, np.float64)
+    nc = o.n_contrib.reshape(o.H, o.W)
+    for t in range(o.gx * o.gy):
+        tx, ty = t % o.gx, t // o.gx
+        blk = nc[ty * 16:(ty + 1) * 16, tx * 16:(tx + 1) * 16].ravel().astype(np.int64)
+        m = int(blk.max()) if blk.size else 0
+        if m == 0:
+            continue
+        at_least = np.cumsum(np.bincount(blk, minlength=m + 1)[::-1])[::-1]  # pixels with count >= v
+        lo = int(o.ranges[t])
+        np.add.at(out, o.gid[lo:lo + m].astype(np.int64), at_least[1:m + 1].astype(np.float64))
+    return out
+
+
+def backward_bounds(o, terms=None) -> dict:
     """Per output element, a bound on the float32 rounding error of the kernels'
     gradients for the oracle `o` after o.backward(..., magnitudes=True). Returns arrays
-    shaped like the outputs of Oracle.backward (None where that output is absent)."""
+    shaped like the outputs of Oracle.backward (None where that output is absent).
+
+    `terms` (per Gaussian, e.g. contribution_counts(o)) replaces the tree-sum depth
+    touched / 8 by the number of terms: the bound of a sum formed in any order, one term
+    at a time (n terms in any order: at most (n - 1) u times the sum of magnitudes), as
+    global atomic accumulation forms it."""
     if getattr(o, "g10abs", None) is None:
         raise RuntimeError("call Oracle.backward(..., magnitudes=True) first")
     k = o._keep
@@ -128,8 +151,8 @@ def backward_bounds(o) -> dict:
         return out
     S = o.g10abs[idx, :10]
     Wt = o.g10abs[idx, 10:]
-    touched = o.touched[idx].astype(np.float64)
-    acc = [B(o.g10[idx, j], U * ((C_SUM + touched / 8.0) * S[:, j] + C_UNWIND * Wt[:, j])) for j in range(10)]
+    spread = o.touched[idx].astype(np.float64) / 8.0 if terms is None else np.asarray(terms, np.float64)[idx]
+    acc = [B(o.g10[idx, j], U * ((C_SUM + spread) * S[:, j] + C_UNWIND * Wt[:, j])) for j in range(10)]
 
     W, H = float(o.W), float(o.H)
     V = [float(x) for x in k["view"]]

@@ -1,5 +1,6 @@
-"""The C ABI library loads and exports every function include/cfgs.h declares; host-side
-validation and workspace sizing work without a GPU."""
+"""The C ABI library loads and exports every function include/cfgs.h and
+include/cfgs_plain.h declare; host-side validation and workspace sizing work without a
+GPU."""
 from __future__ import annotations
 
 import ctypes as C
@@ -22,9 +23,32 @@ def test_library_exports_every_declared_symbol():
     lib = native.load()
     names = _declared("cfgs.h")
     assert len(names) >= 15
-    for n in names:
+    plain = _declared("cfgs_plain.h")
+    assert plain == ["cfgs_plain_backward", "cfgs_plain_bin", "cfgs_plain_render_forward", "cfgs_plain_work_bytes"]
+    for n in names + plain:
         assert hasattr(lib, n), n
-    assert set(native.EXPORTS) <= set(names)
+    assert set(native.EXPORTS) <= set(names) | set(plain)
+
+
+def test_plain_path_rejects_invalid_arguments_on_host():
+    from cfgs import native
+    lib = native.load()
+    assert lib.cfgs_plain_work_bytes(-1, 10, 64, 64) == 0
+    assert lib.cfgs_plain_work_bytes(10, -1, 64, 64) == 0
+    assert lib.cfgs_plain_work_bytes(10, 10, 0, 64) == 0
+    assert lib.cfgs_plain_work_bytes(10, 1 << 31, 64, 64) == 0
+    k = C.c_int64(-5)
+    assert lib.cfgs_plain_bin(None, 10, 1, 1, 10, C.byref(k), None) == 1
+    s = native.Settings()
+    s.image_width, s.image_height = 64, 64
+    assert lib.cfgs_plain_bin(C.byref(s), 10, 1, 1, 10, None, None) == 1
+    assert lib.cfgs_plain_bin(C.byref(s), 10, 1, 1, 1 << 31, C.byref(k), None) == 5
+    assert lib.cfgs_plain_bin(C.byref(s), 0, 1, 1, 10, C.byref(k), None) == 0 and k.value == 0
+    assert lib.cfgs_plain_render_forward(C.byref(s), 10, 1, 1, 1, 10, None, None, None, None) == 1
+    g = native.Gaussians()
+    gr = native.Gradients()
+    assert lib.cfgs_plain_backward(C.byref(s), C.byref(g), None, 1, 1, 1, 10, None, None, None, C.byref(gr),
+                                   None) == 1
 
 
 def test_workspace_sizes_and_layouts():

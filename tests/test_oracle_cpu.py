@@ -180,3 +180,22 @@ def test_c_oracle_edge_scenes():
     assert o.K >= 4 * o.gx * o.gy
     np.testing.assert_array_equal(r["radii"].numpy(), o.radii)
     assert np.abs(r["color"].detach().numpy() - o.color).max() <= 1e-5
+
+
+def test_contribution_counts_match_a_direct_count():
+    """oracle.error_bound.contribution_counts (the term counts of the any-order sum
+    bound) equals a pixel-by-pixel count over the oracle's lists."""
+    from cfgs import scenes
+    from oracle.c_oracle import Oracle
+    from oracle.error_bound import contribution_counts
+    sc = scenes.scene_small(n=800, width=70, height=50, seed=2)
+    o = Oracle.from_scene(sc).forward()
+    want = np.zeros(o.N)
+    for py in range(o.H):
+        for px in range(o.W):
+            t = (py // 16) * o.gx + px // 16
+            for c in range(int(o.n_contrib[py * o.W + px])):
+                want[o.gid[o.ranges[t] + c]] += 1
+    got = contribution_counts(o)
+    np.testing.assert_array_equal(got, want)
+    assert got.sum() == o.n_contrib.sum() > 0
