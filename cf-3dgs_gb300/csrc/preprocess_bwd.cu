@@ -411,22 +411,38 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
       off_l = a.geom.offset[gl];
     }
     const int sub = lane & 7, grp = lane >> 3;
+    // The written marks of this lane's first two instance slots (sub, sub + 8) of all
+    // eight rounds first: sixteen independent byte loads in flight together, so each
+    // round below waits for its records only.
+    uint32_t marks = 0;  // bits 2q, 2q + 1: round q's slots sub, sub + 8
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int src = 4 * q + grp;
+      const uint32_t nt = __shfl_sync(0xffffffffu, nt_l, src);
+      const uint32_t off = __shfl_sync(0xffffffffu, off_l, src);
+      if ((uint32_t)sub < nt && __ldg(a.written + off + sub)) marks |= 1u << (2 * q);
+      if ((uint32_t)sub + 8 < nt && __ldg(a.written + off + sub + 8)) marks |= 2u << (2 * q);
+    }
+    auto add_record = [&](float (&v)[16], uint32_t i) {
+      const float4* rec = a.records + (size_t)kRecordFloat4 * i;
+      const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
+      v[0] += r0.x; v[1] += r0.y; v[2] += r0.z; v[3] += r0.w;
+      v[4] += r1.x; v[5] += r1.y; v[6] += r1.z; v[7] += r1.w;
+      v[8] += r2.x; v[9] += r2.y;
+    };
 #pragma unroll 1
-    for (int gi = 0; gi < 32; gi += 4) {
-      const int src = gi + grp;
+    for (int q = 0; q < 8; ++q) {
+      const int src = 4 * q + grp;
       const uint32_t nt = __shfl_sync(0xffffffffu, nt_l, src);
       const uint32_t off = __shfl_sync(0xffffffffu, off_l, src);
       float v[16];
 #pragma unroll
       for (int k = 0; k < 16; ++k) v[k] = 0.f;
-      for (uint32_t r = sub; r < nt; r += 8) {
-        if (!a.written[off + r]) continue;  // exact-zero record, never written
-        const float4* rec = a.records + (size_t)kRecordFloat4 * (off + r);
-        const float4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
-        v[0] += r0.x; v[1] += r0.y; v[2] += r0.z; v[3] += r0.w;
-        v[4] += r1.x; v[5] += r1.y; v[6] += r1.z; v[7] += r1.w;
-        v[8] += r2.x; v[9] += r2.y;
-      }
+      // slots r = sub, sub + 8, sub + 16, ... in order; unwritten slots are exact zeros
+      if (marks & (1u << (2 * q))) add_record(v, off + sub);
+      if (marks & (2u << (2 * q))) add_record(v, off + sub + 8);
+      for (uint32_t r = sub + 16; r < nt; r += 8)
+        if (a.written[off + r]) add_record(v, off + r);
       group8_sum16(v, lane);
       if (sub < 5) {
         s_acc[warp * 32 + src][2 * sub] = v[0];
