@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
       v[4] += r1.x; v[5] += r1.y; v[6] += r1.z; v[7] += r1.w;
       v[8] += r2.x; v[9] += r2.y;
     };
-#pragma unroll 1
+#pragma unroll 2
     for (int q = 0; q < 8; ++q) {
       const int src = 4 * q + grp;
       const uint32_t nt = __shfl_sync(0xffffffffu, nt_l, src);
