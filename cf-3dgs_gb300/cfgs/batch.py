@@ -163,6 +163,7 @@ class BatchSolver:
         a.lr, a.beta1, a.beta2, a.eps = self.lr, float(self.betas[0]), float(self.betas[1]), self.eps
         # this batch's tuned schedule, else the calling thread's current one
         a.schedule = autotune_mod.c_schedule(self.schedule)
+        a.sh_degree_bound = 1 + max(int(sc.sh_degree) for sc in self.scenes)
         return a
 
     def _counts(self) -> native.Counts:

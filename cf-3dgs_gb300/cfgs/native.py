@@ -100,7 +100,8 @@ class BatchArgs(C.Structure):
                 ("rotations", _vp), ("target", _vp), ("color", _vp), ("radii", _vp), ("geom", _vp), ("image", _vp),
                 ("binning", _vp), ("scratch", _vp), ("pose_partials", _vp), ("xi", _vp), ("adam_state", _vp),
                 ("pose_states", _vp), ("lr", C.c_double), ("beta1", C.c_double), ("beta2", C.c_double),
-                ("eps", C.c_double), ("schedule", RenderSchedule)]
+                ("eps", C.c_double), ("schedule", RenderSchedule), ("sh_degree_bound", C.c_int32),
+                ("pad2_", C.c_int32)]
 
 
 EXPORTS = {

@@ -203,6 +203,10 @@ extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   rb.cap = a->capacity;
   rb.counts = v.iv.counts;
   rb.sched = sched;
+  // Every solve SH degree 0: colour does not depend on the view, so the colour and
+  // opacity sums never reach the pose and the render backward forms the 2D-mean and
+  // conic sums alone (the same bits for those); the records' other terms are zeros.
+  rb.geom_only = a->sh_degree_bound == 1;
   launch_render_bwd(rb, a->num_tiles, st);
 
   PreBwdArgs<SceneTable> pb;

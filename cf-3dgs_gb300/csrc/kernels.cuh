@@ -86,6 +86,7 @@ struct RenderBwdArgs {
   int64_t cap;
   const CfgsCounts* counts;
   CfgsRenderSchedule sched;  // resolved launch shape (resolve_schedule)
+  bool geom_only;            // form only the 2D-mean and conic sums (batched SH-degree-0 pose solves)
 };
 
 template <class Scenes>

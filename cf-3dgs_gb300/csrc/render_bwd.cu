@@ -21,8 +21,10 @@ constexpr int kWarps = kBwdThreads / 32;
 // Sums an instance's per-lane terms over the warp. v[0..7] go through a transposing
 // reduction (each step halves the values a lane carries: 4 + 2 + 1 shuffles, then two
 // plain steps), after which lane L holds the total of v[L >> 2]; v[8] (and v[9] with
-// depth gradients) take plain butterflies, every lane ending with the total.
-template <bool DEPTH>
+// depth gradients) take plain butterflies, every lane ending with the total. With GEOM
+// (only v[0..4] formed, v[5..9] zero) the v[8] butterfly is skipped; the tree that sums
+// v[0..4] is the same either way, so their totals are the same bits.
+template <bool DEPTH, bool GEOM = false>
 __device__ __forceinline__ void warp_reduce_terms(float (&v)[10], int lane) {
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -46,8 +48,10 @@ __device__ __forceinline__ void warp_reduce_terms(float (&v)[10], int lane) {
   }
   v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
   v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+  if (!GEOM) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v[8] += __shfl_xor_sync(0xffffffffu, v[8], o);
+    for (int o = 16; o > 0; o >>= 1) v[8] += __shfl_xor_sync(0xffffffffu, v[8], o);
+  }
   if (DEPTH) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v[9] += __shfl_xor_sync(0xffffffffu, v[9], o);
@@ -127,8 +131,9 @@ __device__ __forceinline__ PairBwd make_pair(const PixelBwd& p, const PixelBwd& 
 // dL/ddepth (w = alpha T). The per-instance factors (opacity, conic) are applied after
 // the reduction (finish_record). A pixel the instance did not reach in the forward pass
 // keeps its state: its factors are 1 (transmittance) and 0 (alpha, G). Returns whether
-// the instance contributed to either pixel.
-template <bool DEPTH>
+// the instance contributed to either pixel. With GEOM only v0..v4 are formed (the terms
+// of dL/dmean2D and dL/dconic; v5..v8 stay zero), with the same operations.
+template <bool DEPTH, bool GEOM = false>
 __device__ __forceinline__ bool unwind_pair(PairBwd& P, int c, float pxf, float2 pyf, const float4& m, const float4& co,
                                             const float4* s_rgbd, int j, float (&v)[10]) {
   const bool in0 = c < (int)P.last0, in1 = c < (int)P.last1;
@@ -155,9 +160,11 @@ __device__ __forceinline__ bool unwind_pair(PairBwd& P, int c, float pxf, float2
   const float2 am = make_float2(a0 ? alpha.x : 0.0f, a1 ? alpha.y : 0.0f);
   P.T = mul2(P.T, inv);
   const float2 w = mul2(am, P.T);
-  v[6] = fmaf(P.dC0.y, w.y, fmaf(P.dC0.x, w.x, v[6]));
-  v[7] = fmaf(P.dC1.y, w.y, fmaf(P.dC1.x, w.x, v[7]));
-  v[8] = fmaf(P.dC2.y, w.y, fmaf(P.dC2.x, w.x, v[8]));
+  if (!GEOM) {
+    v[6] = fmaf(P.dC0.y, w.y, fmaf(P.dC0.x, w.x, v[6]));
+    v[7] = fmaf(P.dC1.y, w.y, fmaf(P.dC1.x, w.x, v[7]));
+    v[8] = fmaf(P.dC2.y, w.y, fmaf(P.dC2.x, w.x, v[8]));
+  }
   const float2 e0 = sub2(splat2(col.x), P.acc0), e1 = sub2(splat2(col.y), P.acc1), e2 = sub2(splat2(col.z), P.acc2);
   float2 dLda = mul2(e0, P.dC0);
   dLda = fma2(e1, P.dC1, dLda);
@@ -175,7 +182,7 @@ __device__ __forceinline__ bool unwind_pair(PairBwd& P, int c, float pxf, float2
   dLda = fma2(mul2(P.T_final, inv), P.dA_bg, dLda);
   const float2 g = mul2(make_float2(a0 ? G.x : 0.0f, a1 ? G.y : 0.0f), dLda);  // d/d opacity
   const float sg = g.x + g.y;
-  v[5] += sg;
+  if (!GEOM) v[5] += sg;
   const float sx = sg * dx;  // both pixels share dx
   const float2 gy = mul2(g, dy);
   v[0] += sx;
@@ -207,7 +214,7 @@ __device__ __forceinline__ void finish_record(float4* rec, const float (&s)[10],
 // (the others' terms are exact zeros). BATCH instances are staged per round; the
 // records do not depend on it (each instance's sums are formed the same way whatever
 // batch it is staged in), so the batch is a schedule choice.
-template <class Scenes, bool DEPTH, int BATCH>
+template <class Scenes, bool DEPTH, int BATCH, bool GEOM = false>
 __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Scenes> a) {
   static_assert(BATCH % 32 == 0 && BATCH <= kBwdThreads, "whole ballot words, one staged instance per thread");
   constexpr int kBwdBatch = BATCH;
@@ -313,9 +320,9 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
         for (int q = 0; q < 10; ++q) v[q] = 0.f;
         const float4 m = s_xyt_b[j];
         const float4 co = s_co_b[j];
-        const bool contrib = unwind_pair<DEPTH>(pp, c, pxf, pyf, m, co, s_rgbd_b, j, v);
+        const bool contrib = unwind_pair<DEPTH, GEOM>(pp, c, pxf, pyf, m, co, s_rgbd_b, j, v);
         if (__ballot_sync(0xffffffffu, contrib)) {
-          warp_reduce_terms<DEPTH>(v, lane);
+          warp_reduce_terms<DEPTH, GEOM>(v, lane);
           if ((lane & 3) == 0) s_part[warp][j][lane >> 2] = v[0];
           if (lane == 0) {
             s_part[warp][j][8] = v[8];
@@ -351,18 +358,19 @@ __global__ void __launch_bounds__(kBwdThreads, 7) k_render_bwd(RenderBwdArgs<Sce
   // Instances at or past the tile's last contributor reach no pixel: nothing to write.
 }
 
-template <class Scenes, bool DEPTH>
+template <class Scenes, bool DEPTH, bool GEOM = false>
 void launch_render_bwd_depth(const RenderBwdArgs<Scenes>& a, int tiles, int batch, cudaStream_t st) {
-  if (batch == 32) k_render_bwd<Scenes, DEPTH, 32><<<tiles, kBwdThreads, 0, st>>>(a);
-  else if (batch == 128) k_render_bwd<Scenes, DEPTH, 128><<<tiles, kBwdThreads, 0, st>>>(a);
-  else k_render_bwd<Scenes, DEPTH, 64><<<tiles, kBwdThreads, 0, st>>>(a);
+  if (batch == 32) k_render_bwd<Scenes, DEPTH, 32, GEOM><<<tiles, kBwdThreads, 0, st>>>(a);
+  else if (batch == 128) k_render_bwd<Scenes, DEPTH, 128, GEOM><<<tiles, kBwdThreads, 0, st>>>(a);
+  else k_render_bwd<Scenes, DEPTH, 64, GEOM><<<tiles, kBwdThreads, 0, st>>>(a);
 }
 
 template <class Scenes>
 void launch_render_bwd(const RenderBwdArgs<Scenes>& a, int tiles, cudaStream_t st) {
   const int batch = a.sched.bwd_batch;
   if constexpr (Scenes::kBatched) {  // batched solves never ask for depth gradients
-    launch_render_bwd_depth<Scenes, false>(a, tiles, batch, st);
+    if (a.geom_only) launch_render_bwd_depth<Scenes, false, true>(a, tiles, batch, st);
+    else launch_render_bwd_depth<Scenes, false>(a, tiles, batch, st);
   } else {
     if (a.dL_ddepth) launch_render_bwd_depth<Scenes, true>(a, tiles, batch, st);
     else launch_render_bwd_depth<Scenes, false>(a, tiles, batch, st);
@@ -408,6 +416,7 @@ extern "C" int cfgs_render_backward(const CfgsSettings* s, int32_t num_gaussians
   ra.cap = capacity;
   ra.counts = iv.counts;
   if (!resolve_schedule(s->schedule, &ra.sched)) return CFGS_ERR_INVALID_ARGUMENT;
+  ra.geom_only = false;
   if (capacity > 0 && cudaMemsetAsync(ra.written, 0, (size_t)capacity, st) != cudaSuccess) return CFGS_ERR_LAUNCH;
   launch_render_bwd(ra, IL.num_tiles, st);
   CFGS_CHECK_LAUNCH(s->debug, st);

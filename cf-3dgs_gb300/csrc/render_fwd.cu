@@ -26,6 +26,7 @@ struct PairFwd {
   bool done0, done1;
 };
 
+template <bool DEPTH>
 __device__ __forceinline__ void composite_pair(PairFwd& p, float pxf, float2 pyf, const float4& xyt, const float4& co,
                                                const float4* s_rgbd, int j, uint32_t pos1) {
   const float2 power = gauss_power2(co.x, co.y, co.z, xyt.x - pxf, sub2(splat2(xyt.y), pyf));
@@ -49,7 +50,7 @@ __device__ __forceinline__ void composite_pair(PairFwd& p, float pxf, float2 pyf
   const float2 C0 = fma2(splat2(c.x), w, p.C0);
   const float2 C1 = fma2(splat2(c.y), w, p.C1);
   const float2 C2 = fma2(splat2(c.z), w, p.C2);
-  const float2 D = fma2(splat2(c.w), w, p.D);
+  const float2 D = DEPTH ? fma2(splat2(c.w), w, p.D) : p.D;
   if (u0) {
     p.C0.x = C0.x;
     p.C1.x = C1.x;
@@ -141,7 +142,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_render_fwd(RenderArgs<Scenes> a)
         const float4 xyt = s_xyt[j];
         const float4 co = s_co[j];
         const uint32_t pos1 = (uint32_t)(base + j + 1);
-        composite_pair(pp, pxf, pyf, xyt, co, s_rgbd, j, pos1);
+        composite_pair<!Scenes::kBatched>(pp, pxf, pyf, xyt, co, s_rgbd, j, pos1);  // batches ask for no depth
       }
     }
   }

@@ -443,6 +443,12 @@ typedef struct CfgsBatchArgs {    /* device pointers of one batch */
   void* pose_states;              /* plan.pose_state_bytes                     */
   double lr, beta1, beta2, eps;
   CfgsRenderSchedule schedule;    /* render kernels' launch shape (zeros: default) */
+  int32_t sh_degree_bound;        /* 1 + the largest SH degree of the solves; 0: not stated.
+                                     1 (every solve SH degree 0, colour independent of the
+                                     view, so only the 2D-mean and conic gradient sums reach
+                                     the pose) lets the render backward form those sums
+                                     alone; any other value forms all of them */
+  int32_t pad2_;
 } CfgsBatchArgs;
 
 /* Sets every solve's pose state from xi (call once before the first iteration). */
