@@ -65,7 +65,8 @@ def _args():
     p.add_argument("--no-plain", action="store_true", help="skip the plain GPU path's iteration")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
     p.add_argument("--workload", default="fwdbwd",
-                   choices=["fwdbwd", "plain", "pose", "pose_iter", "batch", "serve", "ssim", "init", "optim"])
+                   choices=["fwdbwd", "plain", "pose", "pose_iter", "batch", "batch_iter", "serve", "ssim", "init",
+                            "optim"])
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--serve-seconds", type=float, default=60.0)
     p.add_argument("--serve-slots", type=int, default=64)
@@ -704,6 +705,35 @@ def run_pose_iter(a) -> None:
                                  "instance_capacity": int(K0)}}), flush=True)
 
 
+def run_batch_iter(a) -> None:
+    """One iteration of the solve engine on the 64-solve mix, eager launches (no graph):
+    W untimed iterations, then K timed with CUDA events; for profilers."""
+    import torch
+    from cfgs import batch
+    dev = torch.device("cuda", 0)
+    _, probs, _ = _pose_setup(dev, 64)
+    bs = batch.BatchSolver(probs)
+    args = bs.prepare()
+    for _ in range(a.warmup):
+        bs.iterate(args)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("batch_iter")  # lets a profiler take the timed iterations alone
+    t0.record()
+    for _ in range(a.steps):
+        bs.iterate(args)
+    t1.record()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    ms = t0.elapsed_time(t1) / max(a.steps, 1)
+    print(json.dumps({"metric": "pose-solve engine iteration (64 uneven solves, eager launches)",
+                      "value": round(ms, 4), "unit": "ms/iteration", "n_gpus": 1, "steps": a.steps,
+                      "warmup": a.warmup, "higher_is_better": False, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": "64 CF-3DGS pose solves, N log-uniform [5e4,5e5], "
+                                             "320x180/640x360/960x540",
+                                 "instance_capacity": int(bs.capacity)}}), flush=True)
+
+
 def pose_batch(dev, probs, sample: int = 8) -> dict:
     """64 pose solves (N log-uniform in [5e4, 5e5], resolutions 320x180/640x360/960x540)
     batched (one launch per stage, CUDA-graph replays) vs the same solves one after
@@ -1066,6 +1096,8 @@ def main():
         run_pose_iter(a)
     elif a.workload == "batch":
         run_batch(a)
+    elif a.workload == "batch_iter":
+        run_batch_iter(a)
     elif a.workload == "serve":
         run_serve(a)
     elif a.workload == "ssim":

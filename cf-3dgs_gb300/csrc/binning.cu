@@ -319,8 +319,27 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_rank_sums(const uint32_t* 
   if (threadIdx.x == 0) rank_sums[blockIdx.x] = tot;
 }
 
-// One thread per depth-ordered Gaussian; the block's first instance index is the sum
-// of the earlier blocks' rank_sums, the thread's is that plus a block scan. The
+// The per-block instance counts become their exclusive prefix, in place (one block): the
+// emission's first instance index of each block of 256 depth-ordered Gaussians. Run for
+// large batches only: below kRankScanMinBlocks blocks each emission block sums its
+// predecessors itself (cheaper than a launch; quadratic in the block count above it).
+constexpr int kRankScanMinBlocks = 8192;
+inline bool rank_scan_needed(int rank_blocks) { return rank_blocks > kRankScanMinBlocks; }
+__global__ void __launch_bounds__(1024) k_rank_scan(uint32_t* rank_sums, int n) {
+  __shared__ uint32_t sh[64];
+  uint32_t carry = 0, tot;
+  for (int c0 = 0; c0 < n; c0 += blockDim.x) {
+    const int c = c0 + threadIdx.x;
+    const uint32_t v = c < n ? rank_sums[c] : 0u;
+    const uint32_t incl = block_inclusive_scan(v, sh, &tot);
+    if (c < n) rank_sums[c] = carry + incl - v;
+    carry += tot;
+  }
+}
+
+// One thread per depth-ordered Gaussian; the block's first instance index is the sum of
+// the earlier blocks' rank_sums (formed by k_rank_scan for large batches, else by the
+// block itself), the thread's is that plus a block scan. The
 // instances are then written warp-cooperatively: the warp's instances are dealt out
 // 32 per round, one per lane, so the stores of a round are consecutive. In a round, the
 // lanes whose instance ranges meet it mark where their range begins (an OR reduction),
@@ -336,11 +355,16 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_emit(EmitArgs<Scenes> a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.counts->flags, CFGS_FLAG_CAPACITY_OVERFLOW);
     return;
   }
-  uint32_t pre = 0, tot;
+  uint32_t tot, block_first;
+  if (a.rank_scanned) {
+    block_first = a.rank_sums[blockIdx.x];  // exclusive prefix (k_rank_scan)
+  } else {
+    uint32_t pre = 0;
 #pragma unroll 4
-  for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) pre += a.rank_sums[b];
-  block_inclusive_scan(pre, sh, &tot);
-  const uint32_t block_first = tot;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) pre += a.rank_sums[b];
+    block_inclusive_scan(pre, sh, &tot);
+    block_first = tot;
+  }
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t g = 0, nt = 0;
@@ -482,6 +506,7 @@ int launch_depth_order(const GeomView& gv, int64_t slots, cudaStream_t st) {
     }
     const int rank_blocks = (int)((slots + kPreprocessBlock - 1) / kPreprocessBlock);
     k_rank_sums<<<rank_blocks, kPreprocessBlock, 0, st>>>(gv.depth_val[1], gv.touched, slots, gv.rank_sums);
+    if (rank_scan_needed(rank_blocks)) k_rank_scan<<<1, 1024, 0, st>>>(gv.rank_sums, rank_blocks);
   }
   return CFGS_OK;
 }
@@ -500,6 +525,7 @@ int launch_instances(const BinArgs<Scenes>& a, cudaStream_t st) {
     e.total_slots = slots;
     e.order = gv.depth_val[1];
     e.rank_sums = gv.rank_sums;
+    e.rank_scanned = rank_scan_needed(rank_blocks);
     e.geom = gv;
     e.bin = bv;
     e.cap = a.cap;

@@ -36,7 +36,8 @@ struct EmitArgs {
   Scenes scenes;
   int64_t total_slots;
   const uint32_t* order;      // Gaussians in (depth, id) order
-  const uint32_t* rank_sums;  // instances per 256 of them
+  const uint32_t* rank_sums;  // instances per 256 of them (exclusive prefix when rank_scanned)
+  bool rank_scanned;          // k_rank_scan ran (rank_scan_needed)
   GeomView geom;
   BinningView bin;
   int64_t cap;
