@@ -317,6 +317,36 @@ struct ScratchLayout {
 // Scalar math whose exact rounding sequence the CPU oracle reproduces.
 // ---------------------------------------------------------------------------
 
+// Sums six float64 values over the warp by a transposing reduction: each step halves the
+// values a lane carries (4 + 2 + 1 shuffle-and-add steps, then two plain steps), 9 float64
+// adds per lane instead of 30 for six butterflies. Lane 4k ends with the total of value k.
+__device__ __forceinline__ double warp_sum6_f64(const double (&t)[6], int lane) {
+  double v[8] = {t[0], t[1], t[2], t[3], t[4], t[5], 0.0, 0.0};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const bool up = lane & 16;
+    const double send = up ? v[k] : v[k + 4];
+    const double keep = up ? v[k + 4] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const bool up = lane & 8;
+    const double send = up ? v[k] : v[k + 2];
+    const double keep = up ? v[k + 2] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  {
+    const bool up = lane & 4;
+    const double send = up ? v[0] : v[1];
+    const double keep = up ? v[1] : v[0];
+    v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+  v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+  return v[0];
+}
+
 // exp(x) in float: Cody–Waite reduction x = k ln2 + r (|r| <= ln2/2) with ln2 split
 // into a 15-bit head (so k*head is exact) and a tail, then the degree-7 Taylor
 // polynomial of e^r in Horner form (truncation error < 1e-8 relative), then an

@@ -380,11 +380,9 @@ __global__ void __launch_bounds__(256) k_batch_pose_update(const SceneDesc* desc
 #pragma unroll
     for (int k = 0; k < 6; ++k) acc[k] += partials[(size_t)(b0 + b) * 9 + k];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < 6; ++k) {
-    double v = acc[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) s_red[warp][k] = v;
+  {
+    const double tot = warp_sum6_f64(acc, lane);  // lane 4k: partial k of the warp
+    if ((lane & 3) == 0 && (lane >> 2) < 6) s_red[warp][lane >> 2] = tot;
   }
   __syncthreads();
   float* x = xi + 6 * (size_t)s;

@@ -509,33 +509,9 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
     term[4] = q2 * g0 - q0 * g2;
     term[5] = q0 * g1 - q1 * g0;
   }
-  // Warp sums of the six terms by a transposing reduction (float64 adds are scarce on
-  // this part: 9 per lane instead of 30): after it lane 4k holds the total of term k.
   {
-    double v[8] = {term[0], term[1], term[2], term[3], term[4], term[5], 0.0, 0.0};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const bool up = lane & 16;
-      const double send = up ? v[k] : v[k + 4];
-      const double keep = up ? v[k + 4] : v[k];
-      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-      const bool up = lane & 8;
-      const double send = up ? v[k] : v[k + 2];
-      const double keep = up ? v[k + 2] : v[k];
-      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-    {
-      const bool up = lane & 4;
-      const double send = up ? v[0] : v[1];
-      const double keep = up ? v[1] : v[0];
-      v[0] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-    }
-    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
-    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-    if ((lane & 3) == 0 && (lane >> 2) < 6) s_red[warp][lane >> 2] = v[0];
+    const double tot = warp_sum6_f64(term, lane);  // lane 4k: term k of the warp
+    if ((lane & 3) == 0 && (lane >> 2) < 6) s_red[warp][lane >> 2] = tot;
   }
   __syncthreads();
   if (threadIdx.x < 6) {
