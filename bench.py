@@ -440,9 +440,9 @@ def run_e2e(a, dgr, sc, rs, dev, barrier, world) -> dict:
     from pinned host memory and the loss read back every step. `value`: the inputs of
     step i+1 are copied on a second stream into a second set of device buffers while
     step i computes, and step i's loss is read once step i+1 is enqueued (a training
-    loop with host-resident data and asynchronous logging); `serial`: each step copies
-    its own inputs first and reads its loss before the next begins. Both time every
-    step's copies and its loss read-back."""
+    loop with host-resident data and asynchronous logging), the median of three timed
+    windows; `serial`: each step copies its own inputs first and reads its loss before the
+    next begins. Both time every step's copies and its loss read-back."""
     import torch
     from cfgs.loss import l1_loss
     host = {k: getattr(sc, k).pin_memory() for k in ("means3D", "opacities", "shs", "scales", "rotations", "target")}
@@ -524,9 +524,22 @@ def run_e2e(a, dgr, sc, rs, dev, barrier, world) -> dict:
         barrier()
         return max_over_ranks(time.perf_counter() - t0, world, dev)
 
-    dt_serial = timed(lambda: [serial_step() for _ in range(steps)])
-    dt = timed(lambda: run_pipelined(steps))
+    # Host-timed windows of about 60 ms: the collector is paused inside them (a collection
+    # pause would land in one window and not another) and the pipelined figure is the
+    # median of three windows.
+    import gc
+    gc.collect()
+    gc_was_enabled = gc.isenabled()
+    gc.disable()
+    try:
+        dt_serial = timed(lambda: [serial_step() for _ in range(steps)])
+        windows = sorted(timed(lambda: run_pipelined(steps)) for _ in range(3))
+    finally:
+        if gc_was_enabled:
+            gc.enable()
+    dt = windows[1]
     return {"value": round(job_rate(world, steps, dt), 4), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "windows_ms_per_step": [round(w * 1000.0 / steps, 4) for w in windows],
             "d2h_bytes_per_step": 4, "steps": steps, "api": "diff_gaussian_rasterization.GaussianRasterizer",
             "copies": "next step's inputs on a second stream during the current step",
             "loss_read": "every step's loss copied to pinned host memory and read after the next step is enqueued",
