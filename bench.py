@@ -63,6 +63,8 @@ def _args():
     p.add_argument("--no-pose", action="store_true", help="skip the pose-solve half of the metric")
     p.add_argument("--no-tune", action="store_true", help="keep the default render schedule (no autotuning)")
     p.add_argument("--no-plain", action="store_true", help="skip the plain GPU path's iteration")
+    p.add_argument("--bin-launch", type=int, default=0, choices=[0, 1],
+                   help="pose_iter/batch_iter: binning as one launch per stage (0) or one persistent launch (1)")
     p.add_argument("--cpu-budget-s", type=float, default=20.0)
     p.add_argument("--workload", default="fwdbwd",
                    choices=["fwdbwd", "plain", "pose", "pose_iter", "batch", "batch_iter", "serve", "ssim", "init",
@@ -699,6 +701,8 @@ def run_pose_iter(a) -> None:
     dev = torch.device("cuda", 0)
     prob = pose.make_problem(scenes.scene_pose(width=640, height=360, seed=2), dev)
     bs = batch.BatchSolver([prob])
+    from cfgs import autotune
+    autotune.set_schedule(autotune.Schedule(bin_launch=a.bin_launch))
     args = bs.prepare()
     K0 = bs.capacity
     for _ in range(a.warmup):
@@ -715,7 +719,7 @@ def run_pose_iter(a) -> None:
                       "unit": "ms/iteration", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
                       "higher_is_better": False, "dtype": "f32", "data": "synthetic",
                       "config": {"workload": "CF-3DGS relative pose solve, 230400 SH0 Gaussians, 640x360",
-                                 "instance_capacity": int(K0)}}), flush=True)
+                                 "instance_capacity": int(K0), "bin_launch": a.bin_launch}}), flush=True)
 
 
 def run_batch_iter(a) -> None:
@@ -726,6 +730,8 @@ def run_batch_iter(a) -> None:
     dev = torch.device("cuda", 0)
     _, probs, _ = _pose_setup(dev, 64)
     bs = batch.BatchSolver(probs)
+    from cfgs import autotune
+    autotune.set_schedule(autotune.Schedule(bin_launch=a.bin_launch))
     args = bs.prepare()
     for _ in range(a.warmup):
         bs.iterate(args)
@@ -744,7 +750,8 @@ def run_batch_iter(a) -> None:
                       "warmup": a.warmup, "higher_is_better": False, "dtype": "f32", "data": "synthetic",
                       "config": {"workload": "64 CF-3DGS pose solves, N log-uniform [5e4,5e5], "
                                              "320x180/640x360/960x540",
-                                 "instance_capacity": int(bs.capacity)}}), flush=True)
+                                 "instance_capacity": int(bs.capacity), "bin_launch": a.bin_launch}}),
+          flush=True)
 
 
 def pose_batch(dev, probs, sample: int = 8) -> dict:

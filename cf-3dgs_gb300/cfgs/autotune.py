@@ -37,6 +37,7 @@ class Schedule:
     fwd_batch: int = 128
     fwd_warps: int = 4
     bwd_batch: int = 64
+    bin_launch: int = 0  # batched solves: 0 one launch per binning stage, 1 one persistent launch
 
 
 DEFAULT = Schedule()
@@ -50,7 +51,7 @@ _thread = threading.local()
 def c_schedule(s: Schedule | None = None) -> "native.RenderSchedule":
     """The C struct of schedule s (default: the calling thread's current schedule)."""
     s = get_schedule() if s is None else s
-    return native.RenderSchedule(s.fwd_batch, s.fwd_warps, s.bwd_batch, 0)
+    return native.RenderSchedule(s.fwd_batch, s.fwd_warps, s.bwd_batch, s.bin_launch)
 
 
 def set_schedule(s: Schedule) -> None:

@@ -37,9 +37,9 @@ class BatchResult:
 
 
 def _raise_on_timeout(flags: int) -> None:
-    """A kernel's bounded wait for an on-chip copy ran out: the iterations' results are
-    invalid."""
-    if flags & native.FLAG_COPY_TIMEOUT:
+    """A kernel's bounded wait (for an on-chip copy, or the one-launch binning's wait
+    for the other blocks) ran out: the iterations' results are invalid."""
+    if flags & (native.FLAG_COPY_TIMEOUT | native.FLAG_BARRIER_TIMEOUT):
         raise RuntimeError(f"a bounded device wait ran out (flags 0x{flags:x}); the batch's results are invalid")
 
 

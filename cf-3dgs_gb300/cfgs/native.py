@@ -22,13 +22,14 @@ STATUS = {
 FLAG_FRUSTUM_VIOLATION = 0x1
 FLAG_CAPACITY_OVERFLOW = 0x2
 FLAG_COPY_TIMEOUT = 0x4
+FLAG_BARRIER_TIMEOUT = 0x8
 
 _vp = C.c_void_p
 _fp = C.c_void_p  # device float* passed as an address
 
 
 class RenderSchedule(C.Structure):
-    _fields_ = [("fwd_batch", C.c_int32), ("fwd_warps", C.c_int32), ("bwd_batch", C.c_int32), ("reserved", C.c_int32)]
+    _fields_ = [("fwd_batch", C.c_int32), ("fwd_warps", C.c_int32), ("bwd_batch", C.c_int32), ("bin_launch", C.c_int32)]
 
 
 class Settings(C.Structure):

@@ -129,7 +129,8 @@ extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   if (!resolve_schedule(a->schedule, &sched)) return CFGS_ERR_INVALID_ARGUMENT;
   cudaStream_t st = (cudaStream_t)stream;
   BatchViews v = views(a);
-  if (cudaMemsetAsync(v.iv.counts, 0, sizeof(CfgsCounts), st) != cudaSuccess) return CFGS_ERR_LAUNCH;
+  // the counts and the one-launch binning's barrier state (the header's first 256 bytes)
+  if (cudaMemsetAsync(v.iv.counts, 0, 256, st) != cudaSuccess) return CFGS_ERR_LAUNCH;
   if (cudaMemsetAsync(v.iv.tile_count, 0, sizeof(uint32_t) * (size_t)a->num_tiles, st) != cudaSuccess)
     return CFGS_ERR_LAUNCH;
 
@@ -161,7 +162,8 @@ extern "C" int cfgs_batch_iteration(const CfgsBatchArgs* a, void* stream) {
   ba.num_tiles = a->num_tiles;
   ba.tile_count = v.iv.tile_count;
   ba.tile_range = v.iv.tile_range;
-  int status = launch_binning(ba, st);
+  GridBarrier* barrier = reinterpret_cast<GridBarrier*>(reinterpret_cast<char*>(v.iv.counts) + kGridBarrierOffset);
+  int status = sched.bin_launch ? launch_binning_persistent(ba, barrier, st) : launch_binning(ba, st);
   if (status != CFGS_OK) return status;
 
   RenderArgs<SceneTable> ra;

@@ -109,10 +109,10 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d, int bits, unsigned a
 // Digit histogram of one chunk (per-warp shared-memory counters), written to
 // chunk_counts[d][chunk].
 template <int CHUNK, bool DEPTH>
-__global__ void __launch_bounds__(kSortThreads) k_sort_count(SortPass p) {
+__device__ __forceinline__ void sort_count_block(const SortPass& p, uint32_t bid) {
   __shared__ uint32_t hist[kSortWarps][kSortDigits];
   const uint32_t n = pass_elements(p);
-  const uint32_t c0 = blockIdx.x * (uint32_t)CHUNK;
+  const uint32_t c0 = bid * (uint32_t)CHUNK;
   if (c0 >= n) return;
   const int ndig = 1 << p.bits;
   const uint32_t mask = (uint32_t)ndig - 1u;
@@ -135,8 +135,12 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_count(SortPass p) {
     uint32_t s = 0;
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) s += hist[w][d];
-    p.chunk_counts[(size_t)d * p.num_chunks + blockIdx.x] = s;
+    p.chunk_counts[(size_t)d * p.num_chunks + bid] = s;
   }
+}
+template <int CHUNK, bool DEPTH>
+__global__ void __launch_bounds__(kSortThreads) k_sort_count(SortPass p) {
+  sort_count_block<CHUNK, DEPTH>(p, blockIdx.x);
 }
 
 // Block-wide inclusive scan of one value per thread (blockDim.x <= 1024); returns the
@@ -171,10 +175,9 @@ __device__ __forceinline__ uint32_t block_inclusive_scan(uint32_t v, uint32_t* s
 // earlier chunks, and digit_totals[d] the digit's count. The scatter adds the counts of
 // the smaller digits.
 template <int CHUNK>
-__global__ void __launch_bounds__(1024) k_sort_scan(SortPass p) {
+__device__ __forceinline__ void sort_scan_block(const SortPass& p, int d) {
   __shared__ uint32_t sh[64];
   const uint32_t n = pass_elements(p);
-  const int d = blockIdx.x;
   const int64_t nc = ((int64_t)n + CHUNK - 1) / CHUNK;
   uint32_t tot, carry = 0;
   uint32_t* col = p.chunk_counts + (size_t)d * p.num_chunks;
@@ -186,6 +189,10 @@ __global__ void __launch_bounds__(1024) k_sort_scan(SortPass p) {
     carry += tot;
   }
   if (threadIdx.x == 0) p.digit_totals[d] = carry;
+}
+template <int CHUNK>
+__global__ void __launch_bounds__(1024) k_sort_scan(SortPass p) {
+  sort_scan_block<CHUNK>(p, blockIdx.x);
 }
 
 // Shared memory of the scatter: keys and payloads in input order, the permutation
@@ -204,7 +211,7 @@ struct ScatterSmem {
 };
 
 template <int CHUNK, bool DEPTH>
-__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(SortPass p) {
+__device__ __forceinline__ void sort_scatter_block(const SortPass& p, uint32_t bid) {
   using L = ScatterSmem<CHUNK>;
   constexpr int kSlice = CHUNK / kSortWarps;  // elements per warp
   constexpr int kRounds = kSlice / 32;
@@ -220,7 +227,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(SortPass p) {
   __shared__ uint32_t sh[64];
 
   const uint32_t n = pass_elements(p);
-  const uint32_t c0 = blockIdx.x * (uint32_t)CHUNK;
+  const uint32_t c0 = bid * (uint32_t)CHUNK;
   if (c0 >= n) return;
   const int cnt = (int)min((uint32_t)CHUNK, n - c0);
   const int ndig = 1 << p.bits;
@@ -275,7 +282,7 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(SortPass p) {
   const uint32_t below = block_inclusive_scan(dtot, sh, &tot) - dtot;  // elements of smaller digits
   if (t < ndig) {
     s_start[t] = incl - dsum;
-    s_slot[t] = dsum ? below + p.chunk_counts[(size_t)t * p.num_chunks + blockIdx.x] : 0u;
+    s_slot[t] = dsum ? below + p.chunk_counts[(size_t)t * p.num_chunks + bid] : 0u;
   }
   __syncthreads();
 
@@ -307,16 +314,24 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scatter(SortPass p) {
     }
   }
 }
+template <int CHUNK, bool DEPTH>
+__global__ void __launch_bounds__(kSortThreads) k_sort_scatter(SortPass p) {
+  sort_scatter_block<CHUNK, DEPTH>(p, blockIdx.x);
+}
 
 // Instances of every 256 depth-ordered Gaussians (the emission's block prefix).
-__global__ void __launch_bounds__(kPreprocessBlock) k_rank_sums(const uint32_t* order, const uint32_t* touched,
-                                                                int64_t total_slots, uint32_t* rank_sums) {
+__device__ __forceinline__ void rank_sums_block(const uint32_t* order, const uint32_t* touched, int64_t total_slots,
+                                                uint32_t* rank_sums, int bid) {
   __shared__ uint32_t sh[64];
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t r = (int64_t)bid * blockDim.x + threadIdx.x;
   const uint32_t v = r < total_slots ? touched[order[r]] : 0u;
   uint32_t tot;
   block_inclusive_scan(v, sh, &tot);
-  if (threadIdx.x == 0) rank_sums[blockIdx.x] = tot;
+  if (threadIdx.x == 0) rank_sums[bid] = tot;
+}
+__global__ void __launch_bounds__(kPreprocessBlock) k_rank_sums(const uint32_t* order, const uint32_t* touched,
+                                                                int64_t total_slots, uint32_t* rank_sums) {
+  rank_sums_block(order, touched, total_slots, rank_sums, blockIdx.x);
 }
 
 // The per-block instance counts become their exclusive prefix, in place (one block): the
@@ -325,7 +340,7 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_rank_sums(const uint32_t* 
 // predecessors itself (cheaper than a launch; quadratic in the block count above it).
 constexpr int kRankScanMinBlocks = 8192;
 inline bool rank_scan_needed(int rank_blocks) { return rank_blocks > kRankScanMinBlocks; }
-__global__ void __launch_bounds__(1024) k_rank_scan(uint32_t* rank_sums, int n) {
+__device__ __forceinline__ void rank_scan_block(uint32_t* rank_sums, int n) {
   __shared__ uint32_t sh[64];
   uint32_t carry = 0, tot;
   for (int c0 = 0; c0 < n; c0 += blockDim.x) {
@@ -336,6 +351,7 @@ __global__ void __launch_bounds__(1024) k_rank_scan(uint32_t* rank_sums, int n) 
     carry += tot;
   }
 }
+__global__ void __launch_bounds__(1024) k_rank_scan(uint32_t* rank_sums, int n) { rank_scan_block(rank_sums, n); }
 
 // One thread per depth-ordered Gaussian; the block's first instance index is the sum of
 // the earlier blocks' rank_sums (formed by k_rank_scan for large batches, else by the
@@ -348,24 +364,24 @@ __global__ void __launch_bounds__(1024) k_rank_scan(uint32_t* rank_sums, int n) 
 // quotient is estimated with a float reciprocal (off by at most one for j < 2^22) and
 // corrected exactly.
 template <class Scenes>
-__global__ void __launch_bounds__(kPreprocessBlock) k_emit(EmitArgs<Scenes> a) {
+__device__ __forceinline__ void emit_block(const EmitArgs<Scenes>& a, int bid) {
   __shared__ uint32_t sh[64];
   __shared__ uint8_t s_owner[kPreprocessBlock / 32][32];
   if ((int64_t)a.counts->num_rendered > a.cap) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.counts->flags, CFGS_FLAG_CAPACITY_OVERFLOW);
+    if (bid == 0 && threadIdx.x == 0) atomicOr(&a.counts->flags, CFGS_FLAG_CAPACITY_OVERFLOW);
     return;
   }
   uint32_t tot, block_first;
   if (a.rank_scanned) {
-    block_first = a.rank_sums[blockIdx.x];  // exclusive prefix (k_rank_scan)
+    block_first = a.rank_sums[bid];  // exclusive prefix (k_rank_scan)
   } else {
     uint32_t pre = 0;
 #pragma unroll 4
-    for (int b = threadIdx.x; b < (int)blockIdx.x; b += blockDim.x) pre += a.rank_sums[b];
+    for (int b = threadIdx.x; b < bid; b += blockDim.x) pre += a.rank_sums[b];
     block_inclusive_scan(pre, sh, &tot);
     block_first = tot;
   }
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t r = (int64_t)bid * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t g = 0, nt = 0;
   if (r < a.total_slots) {
@@ -436,9 +452,13 @@ __global__ void __launch_bounds__(kPreprocessBlock) k_emit(EmitArgs<Scenes> a) {
     }
   }
 }
+template <class Scenes>
+__global__ void __launch_bounds__(kPreprocessBlock) k_emit(EmitArgs<Scenes> a) {
+  emit_block<Scenes>(a, blockIdx.x);
+}
 
 // Tile ranges from the per-tile instance counts (one block).
-__global__ void __launch_bounds__(1024) k_tile_ranges(const uint32_t* tile_count, uint32_t* tile_range, int num_tiles) {
+__device__ __forceinline__ void tile_ranges_block(const uint32_t* tile_count, uint32_t* tile_range, int num_tiles) {
   __shared__ uint32_t sh[64];
   uint32_t carry = 0, tot;
   for (int base = 0; base < num_tiles; base += blockDim.x) {
@@ -449,6 +469,9 @@ __global__ void __launch_bounds__(1024) k_tile_ranges(const uint32_t* tile_count
     carry += tot;
   }
   if (threadIdx.x == 0) tile_range[num_tiles] = carry;
+}
+__global__ void __launch_bounds__(1024) k_tile_ranges(const uint32_t* tile_count, uint32_t* tile_range, int num_tiles) {
+  tile_ranges_block(tile_count, tile_range, num_tiles);
 }
 
 namespace {
@@ -563,6 +586,177 @@ int launch_instances(const BinArgs<Scenes>& a, cudaStream_t st) {
   k_tile_ranges<<<1, 1024, 0, st>>>(a.tile_count, a.tile_range, a.num_tiles);
   return CFGS_OK;
 }
+
+// ---- the binning as one persistent launch ----------------------------------------------
+// The same block functions as the per-stage kernels above, run by a cooperative grid of
+// resident 256-thread blocks: each stage's blocks are dealt out over the grid, and a
+// bounded grid-wide wait separates the stages (each reads what the previous one wrote).
+// The outputs are the per-stage launches' outputs (integer work, same order).
+template <class Scenes>
+struct PersistentBinArgs {
+  SortPass depth[kDepthPasses];
+  const uint32_t* order;
+  const uint32_t* touched;
+  int64_t slots;
+  uint32_t* rank_sums;
+  int rank_blocks;
+  EmitArgs<Scenes> emit;
+  SortPass tile[kMaxTilePasses];
+  int tile_passes;
+  const uint32_t* tile_count;
+  uint32_t* tile_range;
+  int num_tiles;
+  GridBarrier* barrier;
+  uint32_t* flags;
+};
+
+template <class Scenes>
+__global__ void __launch_bounds__(kSortThreads) k_binning_persistent(PersistentBinArgs<Scenes> a) {
+  static_assert(kSortThreads == kPreprocessBlock && kDepthChunk == kTileChunk, "one block shape for every stage");
+  auto each = [&](int64_t blocks, auto&& block_fn) {
+    for (int64_t b = blockIdx.x; b < blocks; b += gridDim.x) {
+      block_fn((uint32_t)b);
+      __syncthreads();  // the block's shared memory is reused by its next virtual block
+    }
+  };
+  for (int pass = 0; pass < kDepthPasses; ++pass) {
+    const SortPass& p = a.depth[pass];
+    if (pass == 0) each(p.num_chunks, [&](uint32_t b) { sort_count_block<kDepthChunk, true>(p, b); });
+    else each(p.num_chunks, [&](uint32_t b) { sort_count_block<kDepthChunk, false>(p, b); });
+    if (!grid_barrier(a.barrier, a.flags)) return;
+    each(1 << p.bits, [&](uint32_t b) { sort_scan_block<kDepthChunk>(p, (int)b); });
+    if (!grid_barrier(a.barrier, a.flags)) return;
+    if (pass == 0) each(p.num_chunks, [&](uint32_t b) { sort_scatter_block<kDepthChunk, true>(p, b); });
+    else each(p.num_chunks, [&](uint32_t b) { sort_scatter_block<kDepthChunk, false>(p, b); });
+    if (!grid_barrier(a.barrier, a.flags)) return;
+  }
+  each(a.rank_blocks, [&](uint32_t b) { rank_sums_block(a.order, a.touched, a.slots, a.rank_sums, (int)b); });
+  if (!grid_barrier(a.barrier, a.flags)) return;
+  if (a.emit.rank_scanned) {
+    if (blockIdx.x == 0) rank_scan_block(a.rank_sums, a.rank_blocks);
+    if (!grid_barrier(a.barrier, a.flags)) return;
+  }
+  each(a.rank_blocks, [&](uint32_t b) { emit_block<Scenes>(a.emit, (int)b); });
+  if (!grid_barrier(a.barrier, a.flags)) return;
+  for (int pass = 0; pass < a.tile_passes; ++pass) {
+    const SortPass& p = a.tile[pass];
+    each(p.num_chunks, [&](uint32_t b) { sort_count_block<kTileChunk, false>(p, b); });
+    if (!grid_barrier(a.barrier, a.flags)) return;
+    each(1 << p.bits, [&](uint32_t b) { sort_scan_block<kTileChunk>(p, (int)b); });
+    if (!grid_barrier(a.barrier, a.flags)) return;
+    each(p.num_chunks, [&](uint32_t b) { sort_scatter_block<kTileChunk, false>(p, b); });
+    if (!grid_barrier(a.barrier, a.flags)) return;
+  }
+  if (blockIdx.x == 0) tile_ranges_block(a.tile_count, a.tile_range, a.num_tiles);
+}
+
+// The pass descriptions of launch_depth_order and launch_instances, for one launch.
+template <class Scenes>
+int launch_binning_persistent(const BinArgs<Scenes>& a, GridBarrier* barrier, cudaStream_t st) {
+  const GeomView& gv = a.geom;
+  const BinningView& bv = a.bin;
+  const int64_t slots = a.total_slots;
+  if (slots <= 0) return launch_instances(a, st);
+  PersistentBinArgs<Scenes> pa{};
+  int src = -1;
+  for (int pass = 0; pass < kDepthPasses; ++pass) {
+    SortPass& p = pa.depth[pass];
+    const bool last = pass == kDepthPasses - 1;
+    const int dst = src == 0 ? 1 : 0;
+    p.key_in = src < 0 ? nullptr : gv.depth_key[src];
+    p.val_in = src < 0 ? nullptr : gv.depth_val[src];
+    p.depth_rgbd = gv.rgbd;
+    p.depth_touched = gv.touched;
+    p.key_out = last ? nullptr : gv.depth_key[dst];
+    p.val_out = last ? gv.depth_val[1] : gv.depth_val[dst];
+    p.shift = 8 * pass;
+    p.bits = 8;
+    p.n = slots;
+    p.cap = slots;
+    p.num_chunks = sort_chunks(slots, kDepthChunk);
+    p.chunk_counts = gv.depth_counts;
+    p.digit_totals = gv.depth_totals + kSortDigits * pass;
+    src = dst;
+  }
+  const int rank_blocks = (int)((slots + kPreprocessBlock - 1) / kPreprocessBlock);
+  pa.order = gv.depth_val[1];
+  pa.touched = gv.touched;
+  pa.slots = slots;
+  pa.rank_sums = gv.rank_sums;
+  pa.rank_blocks = rank_blocks;
+  EmitArgs<Scenes>& e = pa.emit;
+  e.scenes = a.scenes;
+  e.total_slots = slots;
+  e.order = gv.depth_val[1];
+  e.rank_sums = gv.rank_sums;
+  e.rank_scanned = rank_scan_needed(rank_blocks);
+  e.geom = gv;
+  e.bin = bv;
+  e.cap = a.cap;
+  e.counts = a.counts;
+  int passes, width;
+  tile_sort_plan(a.num_tiles, &passes, &width);
+  if (passes > kMaxTilePasses) return CFGS_ERR_TOO_LARGE;
+  pa.tile_passes = passes;
+  src = 0;
+  for (int pass = 0; pass < passes; ++pass) {
+    SortPass& p = pa.tile[pass];
+    const bool last = pass == passes - 1;
+    const int dst = src ^ 1;
+    p.key_in = bv.key[src];
+    p.val_in = bv.gid[src];
+    p.aux_in = pass == 0 ? nullptr : bv.pidx[src];
+    p.key_out = last ? nullptr : bv.key[dst];
+    p.val_out = last ? bv.sorted_gid : bv.gid[dst];
+    p.aux_out = last ? bv.sorted_pidx : bv.pidx[dst];
+    p.tile_count = last ? a.tile_count : nullptr;
+    p.shift = width * pass;
+    p.bits = width;
+    p.counts = a.counts;
+    p.cap = a.cap;
+    p.num_chunks = sort_chunks(a.cap, kTileChunk);
+    p.chunk_counts = bv.chunk_counts;
+    p.digit_totals = bv.totals + kSortDigits * pass;
+    src = dst;
+  }
+  pa.tile_count = a.tile_count;
+  pa.tile_range = a.tile_range;
+  pa.num_tiles = (int)a.num_tiles;
+  pa.barrier = barrier;
+  pa.flags = &a.counts->flags;
+
+  // every block resident: the grid is the kernel's occupancy times the SM count (per device)
+  const int smem = (int)ScatterSmem<kTileChunk>::bytes(true);
+  static std::atomic<uint64_t> smem_set{0};
+  if (!ensure_dynamic_smem(k_binning_persistent<Scenes>, smem, smem_set)) return CFGS_ERR_LAUNCH;
+  static std::atomic<int> grid_of_device[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return CFGS_ERR_LAUNCH;
+  int grid = dev < 64 ? grid_of_device[dev].load(std::memory_order_acquire) : 0;
+  if (grid <= 0) {
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_binning_persistent<Scenes>, kSortThreads, smem) !=
+            cudaSuccess ||
+        sms <= 0 || per_sm <= 0)
+      return CFGS_ERR_LAUNCH;
+    grid = sms * per_sm;
+    if (dev < 64) grid_of_device[dev].store(grid, std::memory_order_release);
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kSortThreads);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k_binning_persistent<Scenes>, pa) != cudaSuccess) return CFGS_ERR_LAUNCH;
+  return CFGS_OK;
+}
+template int launch_binning_persistent<SceneTable>(const BinArgs<SceneTable>&, GridBarrier*, cudaStream_t);
 
 template <class Scenes>
 int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st) {

@@ -317,6 +317,49 @@ struct ScratchLayout {
 // Scalar math whose exact rounding sequence the CPU oracle reproduces.
 // ---------------------------------------------------------------------------
 
+// Bounded sense-reversing barrier across the blocks of a cooperative launch (every block
+// resident). Lives in the image workspace's header, after CfgsCounts; `arrived` must be
+// zero at launch. A block that waits longer than kGridBarrierMaxPolls polls raises
+// CFGS_FLAG_BARRIER_TIMEOUT and gets false back; its kernel then returns, and the other
+// blocks give up at their next wait the same way.
+struct GridBarrier {
+  unsigned int arrived, generation;
+};
+constexpr size_t kGridBarrierOffset = 128;  // bytes into the image workspace
+static_assert(sizeof(CfgsCounts) <= kGridBarrierOffset && kGridBarrierOffset + sizeof(GridBarrier) <= 256,
+              "the barrier follows the counts inside the 256-byte header");
+constexpr uint32_t kGridBarrierMaxPolls = 1u << 22;
+
+__device__ __forceinline__ bool grid_barrier(GridBarrier* b, uint32_t* flags) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &b->generation;
+    const unsigned int g0 = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(&b->arrived, 1u) == gridDim.x - 1) {  // last to arrive releases the others
+      atomicExch(&b->arrived, 0u);
+      __threadfence();
+      atomicAdd(&b->generation, 1u);
+    } else {
+      uint32_t polls = 0;
+      while (*gen == g0) {
+        if (++polls > kGridBarrierMaxPolls) {
+          ok = 0;
+          atomicOr(flags, CFGS_FLAG_BARRIER_TIMEOUT);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // Sums six float64 values over the warp by a transposing reduction: each step halves the
 // values a lane carries (4 + 2 + 1 shuffle-and-add steps, then two plain steps), 9 float64
 // adds per lane instead of 30 for six butterflies. Lane 4k ends with the total of value k.

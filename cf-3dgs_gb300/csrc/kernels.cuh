@@ -112,6 +112,8 @@ void launch_preprocess(const PreArgs<Scenes>& a, int blocks, cudaStream_t st);
 void launch_scan(uint32_t* block_sums, int num_blocks, CfgsCounts* counts, cudaStream_t st);
 template <class Scenes>
 int launch_binning(const BinArgs<Scenes>& a, cudaStream_t st);
+template <class Scenes>
+int launch_binning_persistent(const BinArgs<Scenes>& a, GridBarrier* barrier, cudaStream_t st);
 int sort_pairs(uint32_t* keys[2], uint32_t* vals[2], int64_t n, int bits, uint32_t* chunk_counts, uint32_t* totals,
                cudaStream_t st, int* result);
 template <class Scenes>

@@ -181,15 +181,16 @@ template void launch_render_fwd<SingleScene>(const RenderArgs<SingleScene>&, int
 template void launch_render_fwd<SceneTable>(const RenderArgs<SceneTable>&, int, cudaStream_t);
 
 bool resolve_schedule(const CfgsRenderSchedule& in, CfgsRenderSchedule* out) {
+  if (in.bin_launch != 0 && in.bin_launch != 1) return false;
   if (in.fwd_batch == 0 && in.fwd_warps == 0 && in.bwd_batch == 0) {
-    *out = CfgsRenderSchedule{kRenderBatch, 4, 64, 0};
+    *out = CfgsRenderSchedule{kRenderBatch, 4, 64, in.bin_launch};
     return true;
   }
   const bool fwd_ok = in.fwd_warps == 4 ? (in.fwd_batch == 64 || in.fwd_batch == 128 || in.fwd_batch == 256)
                                         : (in.fwd_warps == 8 && (in.fwd_batch == 128 || in.fwd_batch == 256));
   const bool bwd_ok = in.bwd_batch == 32 || in.bwd_batch == 64 || in.bwd_batch == 128;
   if (!fwd_ok || !bwd_ok) return false;
-  *out = CfgsRenderSchedule{in.fwd_batch, in.fwd_warps, in.bwd_batch, 0};
+  *out = CfgsRenderSchedule{in.fwd_batch, in.fwd_warps, in.bwd_batch, in.bin_launch};
   return true;
 }
 

@@ -48,6 +48,8 @@ typedef enum CfgsStatus {
 #define CFGS_FLAG_CAPACITY_OVERFLOW 0x2u /* K > binning capacity; outputs are invalid      */
 #define CFGS_FLAG_COPY_TIMEOUT 0x4u      /* a bounded wait for an on-chip copy ran out;   */
                                          /* that call's outputs are invalid               */
+#define CFGS_FLAG_BARRIER_TIMEOUT 0x8u   /* a bounded grid-wide wait of the one-launch    */
+                                         /* binning ran out; outputs are invalid          */
 
 /* Tile size of the screen-space binning (pixels). */
 #define CFGS_TILE_X 16
@@ -63,10 +65,14 @@ typedef enum CfgsStatus {
  *   fwd_warps: warps per tile in the forward: 4 (8x8 pixel boxes, two pixels per
  *              lane) or 8 (8x4 boxes, one pixel per lane; fwd_batch 128 or 256)
  *   bwd_batch: instances staged per round in the backward: 32, 64 or 128
- * All-zero fields mean the default {128, 4, 64}; an unsupported combination makes the
+ *   bin_launch: batched solves only (cfgs_batch_iteration): 0 runs the binning (depth
+ *              sort, emission, tile sort, tile ranges) as one launch per stage, 1 as one
+ *              persistent cooperative launch with a bounded grid-wide wait between
+ *              stages (same outputs)
+ * All-zero fields mean the default {128, 4, 64, 0}; an unsupported combination makes the
  * call return CFGS_ERR_INVALID_ARGUMENT. */
 typedef struct CfgsRenderSchedule {
-  int32_t fwd_batch, fwd_warps, bwd_batch, reserved;
+  int32_t fwd_batch, fwd_warps, bwd_batch, bin_launch;
 } CfgsRenderSchedule;
 
 /* CFGS_OK when `schedule` is supported (zeros: the default), else

@@ -20,6 +20,13 @@ def test_schedule_abi_rejects_unsupported_shapes():
     for good in [(64, 4, 32), (256, 8, 128), (128, 8, 64)]:
         assert lib.cfgs_render_schedule_check(native.C.byref(S(*good, 0)), native.C.byref(r)) == 0
         assert (r.fwd_batch, r.fwd_warps, r.bwd_batch) == good
+    # the binning launch mode: 0 (per stage) or 1 (one persistent launch), kept as given
+    assert lib.cfgs_render_schedule_check(native.C.byref(S(0, 0, 0, 1)), native.C.byref(r)) == 0
+    assert (r.fwd_batch, r.fwd_warps, r.bwd_batch, r.bin_launch) == (128, 4, 64, 1)
+    assert lib.cfgs_render_schedule_check(native.C.byref(S(64, 4, 32, 1)), native.C.byref(r)) == 0
+    assert r.bin_launch == 1
+    for bad_mode in (2, -1):
+        assert lib.cfgs_render_schedule_check(native.C.byref(S(128, 4, 64, bad_mode)), None) == 1
     with pytest.raises(RuntimeError):
         autotune.set_schedule(autotune.Schedule(96, 4, 64))
 
@@ -97,7 +104,8 @@ def test_tune_coordinate_search_and_cache(tmp_path):
     assert calls[7:] == [autotune.DEFAULT, s, autotune.DEFAULT, s]
     data = json.loads(path.read_text())
     (k, e), = data.items()
-    assert k.endswith("|raster/n1/1x1/m1") and e["schedule"] == {"fwd_batch": 256, "fwd_warps": 8, "bwd_batch": 32}
+    assert k.endswith("|raster/n1/1x1/m1") and e["schedule"] == {"fwd_batch": 256, "fwd_warps": 8, "bwd_batch": 32,
+                                                                 "bin_launch": 0}
     assert e["ms"]["256/8/32"] == pytest.approx(6.5)
     # a second tuner on the same file answers from the cache without measuring
     calls.clear()

@@ -89,3 +89,27 @@ def test_prepare_and_iterate_equal_solve(mods):
         bs.iterate(args)
     torch.cuda.synchronize()
     assert np.array_equal(bs.xi.double().cpu().numpy(), ref)
+
+
+def test_one_launch_binning_equals_per_stage_launches(mods):
+    """The binning as one persistent cooperative launch (schedule bin_launch=1) gives the
+    per-stage launches' results bit for bit: through CUDA-graph replays, in direct
+    launches, with a large batch (the emission's offsets from the rank-sum scan), and
+    when an undersized capacity overflows and is retried."""
+    batch, pose, scenes = mods
+    from cfgs import autotune
+    probs = _problems(pose, scenes, SPECS)
+    one = autotune.Schedule(bin_launch=1)
+    ref = batch.BatchSolver(probs, use_graph=False).solve(25)
+    with autotune.using(one):
+        graphed = batch.BatchSolver(probs, graph_chunk=10).solve(25)
+        direct = batch.BatchSolver(probs, use_graph=False).solve(25)
+        small = batch.BatchSolver(probs, use_graph=False, capacity_factor=0.3).solve(25)
+    for r in (graphed, direct, small):
+        assert not r.overflowed
+        assert np.array_equal(r.xi, ref.xi)
+    big = _problems(pose, scenes, [(640, 360, 600_000, 3), (960, 540, 1_000_000, 5), (960, 540, 900_000, 9)])
+    ref_big = batch.BatchSolver(big, use_graph=False).solve(3)
+    with autotune.using(one):
+        one_big = batch.BatchSolver(big, use_graph=False).solve(3)
+    assert np.array_equal(one_big.xi, ref_big.xi)
