@@ -372,15 +372,15 @@ __device__ __forceinline__ void zero_gradients(const PreBwdArgs<Scenes>& a, int6
 // With sh_bulk (degree-3 SH, 16-byte aligned), the block's 256 x 192 bytes of SH
 // coefficients arrive in shared memory by one bulk copy issued before phase 1, and
 // their gradients leave by one bulk store.
-template <class Scenes>
-__global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a) {
+template <class Scenes, bool POSE>
+__global__ void __launch_bounds__(256, POSE ? 4 : 3) k_preprocess_bwd(PreBwdArgs<Scenes> a) {
   extern __shared__ __align__(128) float4 s_sh[];  // [256][12] with sh_bulk
   __shared__ float s_acc[256][11];
   __shared__ double s_red[8][6];
   __shared__ __align__(8) uint64_t s_bar;
   if ((int64_t)a.counts->num_rendered > a.cap) return;  // forward overflowed: outputs untouched
   const SceneDesc& sd = a.scenes.for_block(blockIdx.x);
-  const bool pose_only = a.pose_partials != nullptr;
+  constexpr bool pose_only = POSE;  // a.pose_partials is set exactly for this form
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t blk0 = (int64_t)blockIdx.x * blockDim.x;
   const int M = sd.sh_coeffs;
@@ -526,9 +526,15 @@ __global__ void __launch_bounds__(256, 3) k_preprocess_bwd(PreBwdArgs<Scenes> a)
 template <class Scenes>
 void launch_preprocess_bwd(const PreBwdArgs<Scenes>& a, int blocks, cudaStream_t st) {
   constexpr int kShBulkBytes = 256 * 3 * kMaxShCoeffs * (int)sizeof(float);
-  static std::atomic<uint64_t> smem_set{0};
-  ensure_dynamic_smem(k_preprocess_bwd<Scenes>, kShBulkBytes, smem_set);  // a failure surfaces as a launch error
-  k_preprocess_bwd<Scenes><<<blocks, 256, a.sh_bulk ? kShBulkBytes : 0, st>>>(a);
+  static std::atomic<uint64_t> smem_set{0}, smem_set_pose{0};
+  // a failure of the attribute call surfaces as a launch error
+  if (a.pose_partials) {  // pose-only form: fewer live values, a fourth resident block per SM
+    ensure_dynamic_smem(k_preprocess_bwd<Scenes, true>, kShBulkBytes, smem_set_pose);
+    k_preprocess_bwd<Scenes, true><<<blocks, 256, a.sh_bulk ? kShBulkBytes : 0, st>>>(a);
+  } else {
+    ensure_dynamic_smem(k_preprocess_bwd<Scenes, false>, kShBulkBytes, smem_set);
+    k_preprocess_bwd<Scenes, false><<<blocks, 256, a.sh_bulk ? kShBulkBytes : 0, st>>>(a);
+  }
 }
 template void launch_preprocess_bwd<SingleScene>(const PreBwdArgs<SingleScene>&, int, cudaStream_t);
 template void launch_preprocess_bwd<SceneTable>(const PreBwdArgs<SceneTable>&, int, cudaStream_t);
