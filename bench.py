@@ -215,9 +215,9 @@ def _peaks() -> dict:
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
 # capture of the 1M-Gaussian 1080p workload (metrics that take one pass), at the
 # instance count K it was taken at; scaled by instances for another K.
-NCU_TRAFFIC = {"render_bwd": (177704704 + 80500224, 12433348),
-               "composite": (66821888 + 30515968, 12433348),
-               "preprocess_bwd": (452954624 + 292989184, 12433348)}
+NCU_TRAFFIC = {"render_bwd": (177717504 + 80580864, 12433348),
+               "composite": (67001088 + 30771968, 12433348),
+               "preprocess_bwd": (452126720 + 293896704, 12433348)}
 
 
 def _traffic(kernel: str, K: int):
