@@ -321,3 +321,50 @@ def test_split_binning_equals_one_call(dgr):
                                sc.camera.width, sc.camera.height)
     for k in ("sorted_gid", "sorted_pidx", "tile_range", "offset"):
         assert torch.equal(got[k], ref[k]), k
+
+
+SETTING_CASES = {
+    "white_background": dict(bg=(1.0, 1.0, 1.0), scale=1.0, degree=None),
+    "colour_background_scaled": dict(bg=(0.2, 0.5, 0.8), scale=0.7, degree=None),
+    "sh_degree_1_of_3": dict(bg=None, scale=1.0, degree=1),
+    "sh_degree_2_of_3_scaled": dict(bg=(0.3, 0.3, 0.3), scale=1.3, degree=2),
+}
+
+
+@pytest.mark.parametrize("case", list(SETTING_CASES))
+def test_settings_variants_match_oracle(dgr, case):
+    """The settings the reference varies across training: a white or coloured background
+    (`white_background`), scale_modifier, and an active SH degree below the stored
+    coefficients (the degree rises during training, scene/gaussian_model_cf.py
+    oneupSHdegree). Forward outputs bit-exact, gradients within 1e-4 relative or the
+    float32 bound."""
+    from cfgs import scenes
+    from oracle.c_oracle import Oracle
+    from oracle.error_bound import backward_bounds
+    c = SETTING_CASES[case]
+    sc = scenes.scene_small(n=3000, width=96, height=80, seed=13)
+    if c["bg"] is not None:
+        sc.bg = torch.tensor(c["bg"], dtype=torch.float32)
+    if c["degree"] is not None:
+        sc.sh_degree = c["degree"]
+    rs = settings_for(dgr, sc, scale_modifier=c["scale"])
+    s = sc.to(DEV)
+    leaves = {"means3D": s.means3D.clone().requires_grad_(True),
+              "means2D": torch.zeros_like(s.means3D, requires_grad=True),
+              "opacities": s.opacities.clone().requires_grad_(True), "shs": s.shs.clone().requires_grad_(True),
+              "scales": s.scales.clone().requires_grad_(True), "rotations": s.rotations.clone().requires_grad_(True)}
+    color, radii, depth, alpha = dgr.GaussianRasterizer(rs)(**leaves)
+    H, W = sc.camera.height, sc.camera.width
+    g = torch.Generator().manual_seed(3)
+    gc, gd, ga = torch.randn(3, H, W, generator=g), torch.randn(1, H, W, generator=g), torch.randn(1, H, W, generator=g)
+    torch.autograd.backward([color, depth, alpha], [gc.to(DEV), gd.to(DEV), ga.to(DEV)])
+    torch.cuda.synchronize()
+    ref = Oracle.from_scene(sc, scale_modifier=c["scale"]).forward()
+    np.testing.assert_array_equal(radii.cpu().numpy(), ref.radii)
+    for got, want in ((color, ref.color), (depth, ref.depth), (alpha, ref.alpha)):
+        np.testing.assert_array_equal(bits(got.detach().cpu().numpy()), bits(want))
+    want = ref.backward(gc.numpy(), gd.numpy(), ga.numpy(), magnitudes=True)
+    bound = backward_bounds(ref)
+    for leaf, key in (("means2D", "means2D"), ("opacities", "opacity"), ("means3D", "means3D"), ("shs", "sh"),
+                      ("scales", "scales"), ("rotations", "rotations")):
+        assert_grad_bounded(leaf, leaves[leaf].grad.cpu(), want[key], bound[key])
